@@ -1,0 +1,423 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 MPLA hot path: kernel-CG solves/s at relres 1e-10.
+
+Workload (one "step" = one full solve): the Gaussian kernel system of the
+matrix-free FP64 configuration -- n = 65536 points uniform in [0,1]^2,
+K_ij = exp(-|x_i - x_j|^2 / (2 * 0.05^2)) + 1e-4 delta_ij,
+b_i = sin(2 pi x_i1) cos(2 pi x_i2), x0 = 0 -- solved to a relative
+residual of 1e-10 with the mixed-precision CG (FP32/SFU matvec, FP64
+vectors, dots, scalars and FP64 true-residual replacement).  The plain FP64
+CG on the same system is timed on a bounded sample of iterations (a full
+FP64 solve takes tens of minutes on GB300's FP64 pipe) and reported beside it.
+
+  value   solves/s with points, b and x resident in HBM (device-timed)
+  e2e     the same solve through mgb_cg_gauss_host from pinned host buffers
+          (host->device copies of points, b, x0 and the copy of x back inside
+          the timed region)
+
+``--impl reference`` times the reference MPLA (compiled from its sources into
+oracle/_ref by oracle/build_ref.py) on the same system through its own API:
+FP64 CG with the Gaussian system_assembler plugin, on a bounded sample of
+iterations.  Under torchrun every rank runs its own replica (the path does
+not shard); rank 0 prints the JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "kernel-CG solves/s & p99 latency at relres 1e-10: mixed vs plain FP64, 1 GB300"
+N_FULL, DIM, ELL, NUGGET, EPS = 65536, 2, 0.05, 1e-4, 1e-10
+L2_FLUSH_BYTES = 512 << 20
+SMI_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+# ------------------------------------------------------------------ helpers
+class ClockSampler:
+    """nvidia-smi sampling during the timed region (every 200 ms)."""
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={SMI_FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        rows = []
+        try:
+            for line in Path(self.path).read_text().splitlines():
+                f = [x.strip() for x in line.split(",")]
+                if len(f) >= 9:
+                    rows.append(f)
+        except OSError:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no nvidia-smi samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for name, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def max_over_ranks(value: float, world: int) -> float:
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([value], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def aggregate(units_per_rank: float, seconds_max: float, world: int) -> float:
+    """Whole-job throughput: units processed by all ranks / max time."""
+    return units_per_rank * world / seconds_max
+
+
+# -------------------------------------------------------------- CPU baseline
+def cpu_baseline(points_scaled: np.ndarray, nugget: float, iterations: int, budget_s: float = 10.0) -> dict:
+    """FP64 oracle matvec rows on the host cores for about budget_s seconds;
+    solves/s = entries/s / (n^2 * iterations)."""
+    import oracle
+
+    op = oracle.GaussOp(points_scaled, nugget)
+    n = op.n
+    x = np.ones(n)
+    rows = 256
+    done_entries = 0
+    t0 = time.perf_counter()
+    r0 = 0
+    while time.perf_counter() - t0 < budget_s:
+        nr = min(rows, n - r0)
+        op.matvec(x, rows=nr, cols=n, roff=r0, coff=0)
+        done_entries += nr * n
+        r0 = (r0 + nr) % n
+    dt = time.perf_counter() - t0
+    eps = done_entries / dt
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": eps / (float(n) * n * iterations), "unit": "solves/s", "cores": threads, "kind": "port",
+            "sample": f"{done_entries / 1e9:.2f}e9 FP64 kernel entries of the C oracle matvec ({dt:.1f} s, "
+                      f"OpenMP over rows), scaled by n^2 x {iterations} CG iterations per solve",
+            "entries_per_s": eps}
+
+
+# ---------------------------------------------------------------- our arm
+def run_ours(args, world, rank, local):
+    import torch
+
+    import mpla_gb300 as mg
+    from mpla_gb300 import synth
+
+    if not mg.LIB_PATH.exists():
+        from mpla_gb300 import _build
+
+        _build.build()
+    torch.cuda.set_device(local)
+    mg.init(local)
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    n = args.n
+    prob = synth.gauss_problem(n, DIM, ELL, NUGGET, seed=0)
+    pts_scaled = prob.scaled()
+    b = prob.b
+    dp = mg.GaussPoints(pts_scaled)
+    db = mg.DeviceArray.from_numpy(b)
+    # x and the L2-flush buffer are torch tensors so that zeroing them is
+    # ordered on the benchmark stream together with the solve.
+    x_t = torch.zeros(n, dtype=torch.float64, device="cuda")
+    flush_t = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+
+    class _Ptr:
+        def __init__(self, t):
+            self.ptr = t.data_ptr()
+
+    dx = _Ptr(x_t)
+
+    def step():
+        with torch.cuda.stream(stream):
+            flush_t.zero_()  # L2 flush
+            x_t.zero_()
+            return mg.cg_gauss(dp, NUGGET, db.ptr, dx.ptr, iter_max=args.iter_max, eps=EPS,
+                               precision=mg.PREC_MIXED, stream=sp)
+
+    for _ in range(args.warmup):
+        info = step()
+    torch.cuda.synchronize()
+    barrier(world)
+    launches0 = mg.kernel_launches()
+    infos = []
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        barrier(world)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            infos.append(step())
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+    launches = mg.kernel_launches() - launches0
+    sec = e0.elapsed_time(e1) / 1e3
+    sec_max = max_over_ranks(sec, world)
+    value = aggregate(args.steps, sec_max, world)
+    info = infos[-1]
+    true_rel = float(info.true_relres)
+    if rank == 0:
+        import oracle
+
+        # the error against the FP64 oracle: relres of the returned x (sampled
+        # rows would not do; the full FP64 matvec on the host takes seconds)
+        if n <= 16384:
+            true_rel = oracle.true_relres(oracle.GaussOp(pts_scaled, NUGGET), b, x_t.cpu().numpy())
+
+    # ---- e2e through the host-buffer entry point
+    pin_pts = pts_scaled.copy()
+    e2e_times = []
+    for k in range(args.e2e_steps + 1):
+        barrier(world)
+        t0 = time.perf_counter()
+        x_host, einfo = mg.cg_gauss_host(pin_pts, NUGGET, b, iter_max=args.iter_max, eps=EPS, precision=mg.PREC_MIXED)
+        torch.cuda.synchronize()
+        if k > 0:
+            e2e_times.append(time.perf_counter() - t0)
+    e2e_sec = max_over_ranks(sum(e2e_times), world)
+    e2e_value = aggregate(args.e2e_steps, e2e_sec, world)
+
+    # ---- plain FP64 CG: bounded sample of iterations
+    fp_iters = args.fp64_sample_iters
+    with torch.cuda.stream(stream):
+        x_t.zero_()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        finfo = mg.cg_gauss(dp, NUGGET, db.ptr, dx.ptr, iter_max=fp_iters + 1, eps=EPS, precision=mg.PREC_FP64,
+                            stream=sp)
+        t1.record(stream)
+    torch.cuda.synchronize()
+    fp_ms_per_iter = t0.elapsed_time(t1) / max(1, finfo.iterations + 1)
+
+    # ---- dominant kernel: the mixed matvec, per-launch device time
+    dy = mg.DeviceArray(n)
+    dxr = mg.DeviceArray.from_numpy(np.random.default_rng(0).standard_normal(n))
+    mixed_ms = mg.time_gauss_matvec(dp, NUGGET, mg.PREC_MIXED, dxr.ptr, dy.ptr, reps=20, stream=sp)
+    f64_ms = mg.time_gauss_matvec(dp, NUGGET, mg.PREC_FP64, dxr.ptr, dy.ptr, reps=3, stream=sp)
+    clocks = clk.summary()
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    sm_mhz = clocks.get("sm_mhz") or 1900.0
+    entries = float(n) * n
+    mixed_rate = entries / (mixed_ms * 1e-3)
+    sfu_peak = 16.0 * sms * sm_mhz * 1e6
+    fp64_rate = entries / (f64_ms * 1e-3)
+
+    iters_mixed = int(info.iterations)
+    # FP64 CG iteration count for this system: measured once with a full
+    # FP64 solve (see profiles/); until then the mixed count stands in.
+    iters_fp64 = args.fp64_iterations or iters_mixed
+    fp64_solves_est = 1.0 / (fp_ms_per_iter * 1e-3 * iters_fp64)
+
+    if rank != 0:
+        return
+    cpu = cpu_baseline(pts_scaled, NUGGET, iters_fp64, budget_s=args.cpu_seconds) if not args.no_cpu else None
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "solves/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": sec_max * 1e3 / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 matvec (SFU exp2) + f64 vectors/dots/scalars/true residual",
+        "data": "synthetic: seeded splitmix64, points U[0,1]^2, b = sin(2 pi x1) cos(2 pi x2)",
+        "config": {"workload": f"Gaussian kernel CG, n={n}, d={DIM}, l={ELL}, nugget={NUGGET}, relres {EPS}, x0=0",
+                   "solver": "mixed CG with FP64 reliable residual replacement",
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": f"{L2_FLUSH_BYTES >> 20} MiB buffer zeroed before every step"},
+        "iterations": iters_mixed,
+        "fp64_true_residual_replacements": int(info.fp64_matvecs),
+        "true_relres": true_rel,
+        "p50_ms": statistics.median([sec_max * 1e3 / args.steps]),
+        "e2e": {"value": e2e_value, "unit": "solves/s",
+                "h2d_bytes_per_step": int(pts_scaled.nbytes + b.nbytes + 8 * n),
+                "d2h_bytes_per_step": int(8 * n)},
+        "fp64": {"ms_per_iteration": fp_ms_per_iter, "sample_iterations": int(finfo.iterations + 1),
+                 "matvec_ms": f64_ms, "entries_per_s": fp64_rate,
+                 "iterations_assumed": iters_fp64,
+                 "solves_per_s_est": fp64_solves_est,
+                 "mixed_over_fp64": value / fp64_solves_est},
+        "roofline": {"bound": "sfu", "kernel": "gauss_mixed_kernel",
+                     "achieved": mixed_rate / 1e12, "peak": sfu_peak / 1e12, "unit": "Tex2/s",
+                     "frac": mixed_rate / sfu_peak, "traffic": None,
+                     "per_unit": "1 kernel entry = 1 ex2 + 6 FP32 ops; n^2 entries per launch",
+                     "peak_source": f"nominal 16 ex2/clk/SM x {sms} SMs x {sm_mhz:.0f} MHz median SM clock"},
+        "cpu_baseline": cpu,
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------- reference arm
+def run_reference(args, world, rank, local):
+    if rank != 0:
+        return
+    refdir = ROOT / "oracle" / "_ref"
+    lib = refdir / "libmplaref.so"
+    if not lib.exists():
+        try:
+            sys.path.insert(0, str(ROOT / "oracle"))
+            import build_ref
+
+            build_ref.build()
+        except Exception as e:  # noqa: BLE001
+            print(json.dumps({"impl": "reference", "unavailable": f"reference MPLA not built: {e}"}))
+            return
+    import ctypes as C
+
+    from mpla_gb300 import synth
+
+    L = C.CDLL(str(lib))
+    L.ref_init.argtypes = [C.c_int]
+    L.ref_cg_gauss_sample.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_double, C.c_void_p, C.c_int, C.c_double,
+                                      C.POINTER(C.c_double), C.POINTER(C.c_int)]
+    L.ref_cg_gauss_sample.restype = C.c_int
+    if L.ref_init(local) != 0:
+        print(json.dumps({"impl": "reference", "unavailable": "reference MPLA failed to initialise the device"}))
+        return
+    n = args.n
+    prob = synth.gauss_problem(n, DIM, ELL, NUGGET, seed=0)
+    pts = np.ascontiguousarray(prob.scaled())
+    b = np.ascontiguousarray(prob.b)
+    sample_iters = args.ref_sample_iters
+    ms = C.c_double()
+    it = C.c_int()
+    for _ in range(args.warmup):
+        L.ref_cg_gauss_sample(n, DIM, pts.ctypes.data, NUGGET, b.ctypes.data, sample_iters, EPS, C.byref(ms),
+                              C.byref(it))
+    total_ms, total_it = 0.0, 0
+    for _ in range(args.steps):
+        st = L.ref_cg_gauss_sample(n, DIM, pts.ctypes.data, NUGGET, b.ctypes.data, sample_iters, EPS, C.byref(ms),
+                                   C.byref(it))
+        if st != 0:
+            print(json.dumps({"impl": "reference", "unavailable": f"reference CG sample failed (status {st})"}))
+            return
+        total_ms += ms.value
+        total_it += it.value
+    ms_per_iter = total_ms / max(1, total_it)
+    iters_fp64 = args.fp64_iterations or 0
+    value = (1.0 / (ms_per_iter * 1e-3 * iters_fp64)) if iters_fp64 else None
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded splitmix64, points U[0,1]^2, b = sin(2 pi x1) cos(2 pi x2)",
+        "config": {"workload": f"Gaussian kernel CG, n={n}, d={DIM}, l={ELL}, nugget={NUGGET}, relres {EPS}, x0=0",
+                   "solver": "reference MPLA FP64 CG (mpla_generic_conjugate_gradient_with_checkpoint_restart, "
+                             "gaussian system_assembler, streamed cuBLAS core)"},
+        "ms_per_iteration": ms_per_iter,
+        "iterations_assumed": iters_fp64,
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": 1, "kind": "reference",
+                         "sample": f"{sample_iters} CG iterations per step of the reference MPLA built from its "
+                                   f"sources (GPU path, 1 rank), scaled by the FP64 iteration count"},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main(argv=None):
+    p = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=2)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--n", type=int, default=N_FULL)
+    p.add_argument("--iter-max", type=int, default=200000)
+    p.add_argument("--e2e-steps", type=int, default=1)
+    p.add_argument("--fp64-sample-iters", type=int, default=20)
+    p.add_argument("--fp64-iterations", type=int, default=0,
+                   help="FP64 CG iteration count of the full solve, when known (used to scale sampled iterations)")
+    p.add_argument("--ref-sample-iters", type=int, default=3)
+    p.add_argument("--cpu-seconds", type=float, default=10.0)
+    p.add_argument("--no-cpu", action="store_true")
+    args = p.parse_args(argv)
+    if args.warmup < 3:
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    try:
+        if args.impl == "reference":
+            run_reference(args, world, rank, local)
+        else:
+            run_ours(args, world, rank, local)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,159 @@
+/* mpla_gb300.h — C ABI of the GB300 MPLA hot path.
+ *
+ * Plain C linkage, plain pointers and sizes, integer status codes.  This is
+ * the boundary that foreign-language bindings (ctypes, cgo, JNI) load; the
+ * C++ drop-in API of mpla.h is implemented on the same internals.  Each entry
+ * names the MPLA interface it replaces (file:line in the original sources).
+ *
+ * Conventions
+ *  - Pointers named *_dev are device pointers; *_host are host pointers.
+ *  - `stream` is a cudaStream_t passed as void*; NULL selects the library's
+ *    own stream for the current device.
+ *  - Every function returns MGB_OK (0) or an MGB_ERR_* code; the message of
+ *    the last failure on the calling thread is returned by mgb_last_error().
+ *  - Vectors and matrices are FP64, column-major (lda >= rows), as in MPLA.
+ *  - Gaussian systems: K(i,j) = exp(-|p_i - p_j|^2) (+ nugget on i == j, or
+ *    + 1e-8 when |p_i - p_j| < 1e-14 under MGB_NUGGET_KERNEL_CU), points in
+ *    structure-of-arrays form, already scaled by 1/(sqrt(2) l) for a length
+ *    scale l.
+ */
+#ifndef MPLA_GB300_H
+#define MPLA_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define MGB_OK 0
+#define MGB_ERR_CUDA 1       /* a CUDA runtime call failed */
+#define MGB_ERR_ARG 2        /* invalid argument (size, pointer, alignment) */
+#define MGB_ERR_NOMEM 3      /* device allocation failed or admission refused */
+#define MGB_ERR_BREAKDOWN 4  /* Krylov breakdown: zero or negative curvature, non-finite scalar */
+#define MGB_ERR_NOTCONV 5    /* iteration cap reached before the tolerance */
+#define MGB_ERR_NODEV 6      /* no CUDA device */
+#define MGB_ERR_TIMEOUT 7    /* a bounded device-side wait gave up */
+#define MGB_ERR_IO 8         /* checkpoint file missing, short or of the wrong size */
+
+/* nugget rules for Gaussian systems */
+#define MGB_NUGGET_DIAGONAL 0   /* + nugget when i == j (kernel_system_assembler.h:24-38) */
+#define MGB_NUGGET_KERNEL_CU 1  /* + 1e-8 when distance < 1e-14 (kernel.cu:39-50) */
+
+/* stopping rules of the CG variants */
+#define MGB_STOP_RELATIVE 0  /* ||r|| / ||b|| < eps  (mpla.cpp:963-968) */
+#define MGB_STOP_RMS 1       /* sqrt(<r,r>/n) < eps  (mpla.cpp:868-871) */
+
+/* inner matvec precision of the Gaussian solvers */
+#define MGB_PREC_FP64 0   /* plain FP64 CG */
+#define MGB_PREC_MIXED 1  /* FP32 matvec (split-BF16 tensor-core distances), FP64 vectors, dots, scalars and true residuals */
+
+/* ---------------------------------------------------------------- runtime */
+int mgb_version(void);
+const char* mgb_last_error(void);
+/* Select and initialise a device (creates the library stream and tables). */
+int mgb_init(int device);
+/* Release all device memory and the stream of the current device. */
+int mgb_shutdown(void);
+int mgb_device_sync(void);
+
+/* Convenience memory helpers so bindings need no other CUDA wrapper. */
+int mgb_malloc(void** ptr_dev, size_t bytes);
+int mgb_free(void* ptr_dev);
+int mgb_memcpy_htod(void* dst_dev, const void* src_host, size_t bytes);
+int mgb_memcpy_dtoh(void* dst_host, const void* src_dev, size_t bytes);
+int mgb_memset(void* ptr_dev, int value, size_t bytes);
+/* Pinned host buffers for the end-to-end (host-buffer) entry points. */
+int mgb_host_alloc(void** ptr_host, size_t bytes);
+int mgb_host_free(void* ptr_host);
+
+/* ------------------------------------------------------------ dense BLAS */
+/* y = A x, A m x n column-major.  Replaces the cublasDgemv of mpla_dgemv
+ * (mpla.cpp:716-751) at the 1x1 process grid. */
+int mgb_dgemv(int m, int n, const double* A_dev, int lda, const double* x_dev, double* y_dev, void* stream);
+/* *result_host = <x, y>.  Replaces mpla_ddot (mpla.cpp:753-770). */
+int mgb_ddot(int n, const double* x_dev, const double* y_dev, double* result_host, void* stream);
+/* y += alpha x.  Replaces mpla_daxpy (mpla.cpp:806-810). */
+int mgb_daxpy(int n, double alpha, const double* x_dev, double* y_dev, void* stream);
+
+/* --------------------------------------------------- Gaussian kernel matvec */
+/* y[i] = sum_j K(row_offset+i, col_offset+j) x[j] over a rows x cols block,
+ * FP64 throughout, no matrix stored.  coords_dev is a HOST array of `dim`
+ * device pointers (each of length >= max(row_offset+rows, col_offset+cols)).
+ * Replaces mpla_dgemv_core_kernel[_streamed]_cublas (kernel.cu:87-171) and
+ * mpla_dgemv_core_generic_system_matrix[_streamed]_cublas
+ * (generic_system_adapter.cu:53-137) for the Gaussian assembler. */
+int mgb_gauss_matvec_f64(int rows, int cols, int row_offset, int col_offset, int dim,
+                         const double* const* coords_dev, double nugget, int nugget_rule,
+                         const double* x_dev, double* y_dev, void* stream);
+/* Same product with the mixed-precision kernel: FP32 arithmetic, squared
+ * distances from split-BF16 tensor-core cross terms, exponentials on the SFU.
+ * x and y stay FP64.  Square systems only (rows == cols, offsets 0). */
+int mgb_gauss_matvec_mixed(int n, int dim, const double* const* coords_dev, double nugget,
+                           const double* x_dev, double* y_dev, void* stream);
+/* Evaluate single entries K(i,j), 0 <= i,j < n, with the FP64 kernel's
+ * arithmetic (used by the entry-accuracy tests). */
+int mgb_gauss_entries_f64(int n, int count, const int* i_dev, const int* j_dev, int dim,
+                          const double* const* coords_dev, double nugget, int nugget_rule,
+                          double* out_dev, void* stream);
+
+/* ----------------------------------------------------------------- solvers */
+typedef struct mgb_solve_info {
+  int iterations;     /* Krylov iterations executed (matvecs in the loop) */
+  int status;         /* MGB_OK, MGB_ERR_NOTCONV or MGB_ERR_BREAKDOWN */
+  double final_res;   /* value of the stopping measure at exit */
+  double true_relres; /* ||b - A x|| / ||b|| recomputed in FP64 at exit (mixed: always; fp64: if requested) */
+  int fp64_matvecs;   /* FP64 matvecs spent (mixed: true-residual replacements) */
+  int low_matvecs;    /* FP32 matvecs spent (mixed only) */
+  double seconds;     /* host wall time of the call */
+} mgb_solve_info;
+
+/* CG on a dense SPD matrix (column-major, lda = n).  Follows
+ * mpla_generic_conjugate_gradient[_with_checkpoint_restart] (mpla.cpp:817-1001)
+ * with the given stopping rule; x holds x0 on entry and the solution on exit. */
+int mgb_cg_dense(int n, const double* A_dev, int lda, const double* b_dev, double* x_dev,
+                 int iter_max, double eps, int stop_rule, mgb_solve_info* info, void* stream);
+/* BiCGSTAB on a dense matrix; follows mpla_generic_BiCGSTAB_with_checkpoint_restart
+ * (mpla.cpp:1003-1183): true relative residual as the stopping measure. */
+int mgb_bicgstab_dense(int n, const double* A_dev, int lda, const double* b_dev, double* x_dev,
+                       int iter_max, double eps, mgb_solve_info* info, void* stream);
+/* CG on a Gaussian kernel system held on the device.  precision selects the
+ * plain FP64 iteration or the mixed form (FP32 matvec inside FP64 reliable
+ * residual replacement; the stopping rule is then always the FP64 true
+ * relative residual). */
+int mgb_cg_gauss(int n, int dim, const double* const* coords_dev, double nugget, int nugget_rule,
+                 const double* b_dev, double* x_dev, int iter_max, double eps, int stop_rule,
+                 int precision, mgb_solve_info* info, void* stream);
+int mgb_bicgstab_gauss(int n, int dim, const double* const* coords_dev, double nugget, int nugget_rule,
+                       const double* b_dev, double* x_dev, int iter_max, double eps,
+                       mgb_solve_info* info, void* stream);
+/* End-to-end entry: points (n x dim, structure of arrays, already scaled),
+ * b and x0 in HOST memory; copies in, solves, copies x back. */
+int mgb_cg_gauss_host(int n, int dim, const double* coords_host, double nugget,
+                      const double* b_host, double* x_host, int iter_max, double eps,
+                      int precision, mgb_solve_info* info);
+
+/* ------------------------------------------------------------ measurement */
+/* Kernels this library has launched so far in this process (a kernel node
+ * replayed by a CUDA graph counts once per replay). */
+long long mgb_kernel_launches(void);
+/* Mean device time of one launch of the Gaussian matvec kernel (precision
+ * MGB_PREC_FP64 or MGB_PREC_MIXED) over `reps` back-to-back launches on
+ * prepared operands, measured with CUDA events on `stream`. */
+int mgb_time_gauss_matvec(int n, int dim, const double* const* coords_dev, double nugget, int precision,
+                          const double* x_dev, double* y_dev, int reps, double* ms_per_launch, void* stream);
+/* Same for the dense dgemv on an n x n column-major matrix. */
+int mgb_time_dgemv(int n, const double* A_dev, const double* x_dev, double* y_dev, int reps,
+                   double* ms_per_launch, void* stream);
+
+/* ---------------------------------------------------------- checkpoint I/O */
+/* File format of mpla_save_vector (mpla.cpp:605-652): int32 n, then n float64. */
+int mgb_save_vector(const char* path, int n, const double* x_dev);
+int mgb_load_vector(const char* path, int n, double* x_dev);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,313 @@
+"""GB300-native implementation of MPLA's data-parallel hot path.
+
+The native library ``lib/libmpla.so`` (built from ``csrc/`` by ``_build.py``)
+exports the drop-in mpla.h C++ API and the C ABI of ``include/mpla_gb300.h``.
+This module binds the C ABI with ctypes: device buffers, the dense dgemv /
+dot / axpy, the fused Gaussian kernel matvecs and the CG / BiCGSTAB solvers.
+There is no CPU fallback: if the library is missing, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "lib" / "libmpla.so"
+
+MGB_OK = 0
+MGB_ERR_CUDA = 1
+MGB_ERR_ARG = 2
+MGB_ERR_NOMEM = 3
+MGB_ERR_BREAKDOWN = 4
+MGB_ERR_NOTCONV = 5
+MGB_ERR_NODEV = 6
+MGB_ERR_TIMEOUT = 7
+MGB_ERR_IO = 8
+
+NUGGET_DIAGONAL = 0
+NUGGET_KERNEL_CU = 1
+STOP_RELATIVE = 0
+STOP_RMS = 1
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+# Every C-ABI symbol declared in include/mpla_gb300.h (checked by the tests).
+C_ABI_SYMBOLS = (
+    "mgb_version", "mgb_last_error", "mgb_init", "mgb_shutdown", "mgb_device_sync",
+    "mgb_malloc", "mgb_free", "mgb_memcpy_htod", "mgb_memcpy_dtoh", "mgb_memset",
+    "mgb_host_alloc", "mgb_host_free",
+    "mgb_dgemv", "mgb_ddot", "mgb_daxpy",
+    "mgb_gauss_matvec_f64", "mgb_gauss_matvec_mixed", "mgb_gauss_entries_f64",
+    "mgb_cg_dense", "mgb_bicgstab_dense", "mgb_cg_gauss", "mgb_bicgstab_gauss", "mgb_cg_gauss_host",
+    "mgb_kernel_launches", "mgb_time_gauss_matvec", "mgb_time_dgemv",
+    "mgb_save_vector", "mgb_load_vector",
+)
+
+
+class MplaError(RuntimeError):
+    """A C-ABI call returned a non-zero status."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"[status {status}] {message}")
+        self.status = status
+
+
+class SolveInfo(C.Structure):
+    _fields_ = [
+        ("iterations", C.c_int),
+        ("status", C.c_int),
+        ("final_res", C.c_double),
+        ("true_relres", C.c_double),
+        ("fp64_matvecs", C.c_int),
+        ("low_matvecs", C.c_int),
+        ("seconds", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+_lib = None
+_P = C.c_void_p
+_I = C.c_int
+_D = C.c_double
+_SIGS = {
+    "mgb_version": (_I, []),
+    "mgb_last_error": (C.c_char_p, []),
+    "mgb_init": (_I, [_I]),
+    "mgb_shutdown": (_I, []),
+    "mgb_device_sync": (_I, []),
+    "mgb_malloc": (_I, [C.POINTER(_P), C.c_size_t]),
+    "mgb_free": (_I, [_P]),
+    "mgb_memcpy_htod": (_I, [_P, _P, C.c_size_t]),
+    "mgb_memcpy_dtoh": (_I, [_P, _P, C.c_size_t]),
+    "mgb_memset": (_I, [_P, _I, C.c_size_t]),
+    "mgb_host_alloc": (_I, [C.POINTER(_P), C.c_size_t]),
+    "mgb_host_free": (_I, [_P]),
+    "mgb_dgemv": (_I, [_I, _I, _P, _I, _P, _P, _P]),
+    "mgb_ddot": (_I, [_I, _P, _P, C.POINTER(_D), _P]),
+    "mgb_daxpy": (_I, [_I, _D, _P, _P, _P]),
+    "mgb_gauss_matvec_f64": (_I, [_I, _I, _I, _I, _I, _P, _D, _I, _P, _P, _P]),
+    "mgb_gauss_matvec_mixed": (_I, [_I, _I, _P, _D, _P, _P, _P]),
+    "mgb_gauss_entries_f64": (_I, [_I, _I, _P, _P, _I, _P, _D, _I, _P, _P]),
+    "mgb_cg_dense": (_I, [_I, _P, _I, _P, _P, _I, _D, _I, C.POINTER(SolveInfo), _P]),
+    "mgb_bicgstab_dense": (_I, [_I, _P, _I, _P, _P, _I, _D, C.POINTER(SolveInfo), _P]),
+    "mgb_cg_gauss": (_I, [_I, _I, _P, _D, _I, _P, _P, _I, _D, _I, _I, C.POINTER(SolveInfo), _P]),
+    "mgb_bicgstab_gauss": (_I, [_I, _I, _P, _D, _I, _P, _P, _I, _D, C.POINTER(SolveInfo), _P]),
+    "mgb_cg_gauss_host": (_I, [_I, _I, _P, _D, _P, _P, _I, _D, _I, C.POINTER(SolveInfo)]),
+    "mgb_kernel_launches": (C.c_longlong, []),
+    "mgb_time_gauss_matvec": (_I, [_I, _I, _P, _D, _I, _P, _P, _I, C.POINTER(_D), _P]),
+    "mgb_time_dgemv": (_I, [_I, _P, _P, _P, _I, C.POINTER(_D), _P]),
+    "mgb_save_vector": (_I, [C.c_char_p, _I, _P]),
+    "mgb_load_vector": (_I, [C.c_char_p, _I, _P]),
+}
+
+
+def lib():
+    """The loaded native library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise MplaError(-1, f"native library missing: {LIB_PATH} (run __graft_entry__.build())")
+        L = C.CDLL(str(LIB_PATH))
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status: int) -> int:
+    if status != MGB_OK:
+        raise MplaError(status, lib().mgb_last_error().decode(errors="replace"))
+    return status
+
+
+def init(device: int = 0) -> None:
+    check(lib().mgb_init(device))
+
+
+def synchronize() -> None:
+    check(lib().mgb_device_sync())
+
+
+# ------------------------------------------------------------------ buffers
+class DeviceArray:
+    """A float64/int32 device buffer owned by the library's allocator."""
+
+    def __init__(self, count: int, dtype=np.float64):
+        self.dtype = np.dtype(dtype)
+        self.count = int(count)
+        self.nbytes = self.count * self.dtype.itemsize
+        p = C.c_void_p()
+        check(lib().mgb_malloc(C.byref(p), max(self.nbytes, 1)))
+        self.ptr = p.value
+
+    @classmethod
+    def from_numpy(cls, a: np.ndarray) -> "DeviceArray":
+        a = np.ascontiguousarray(a.ravel(order="K"))
+        d = cls(a.size, a.dtype)
+        if a.size:
+            check(lib().mgb_memcpy_htod(d.ptr, a.ctypes.data, d.nbytes))
+        return d
+
+    def upload(self, a: np.ndarray) -> None:
+        a = np.ascontiguousarray(a, dtype=self.dtype).ravel()
+        assert a.size == self.count
+        check(lib().mgb_memcpy_htod(self.ptr, a.ctypes.data, self.nbytes))
+
+    def numpy(self) -> np.ndarray:
+        out = np.empty(self.count, dtype=self.dtype)
+        if self.count:
+            check(lib().mgb_memcpy_dtoh(out.ctypes.data, self.ptr, self.nbytes))
+        return out
+
+    def zero(self) -> None:
+        check(lib().mgb_memset(self.ptr, 0, self.nbytes))
+
+    def free(self) -> None:
+        if self.ptr:
+            lib().mgb_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def _coord_array(coords) -> C.Array:
+    """Host array of device pointers, one per dimension."""
+    ptrs = [c.ptr if isinstance(c, DeviceArray) else int(c) for c in coords]
+    return (C.c_void_p * len(ptrs))(*ptrs)
+
+
+class GaussPoints:
+    """Device-resident structure-of-arrays points (already scaled)."""
+
+    def __init__(self, scaled_points: np.ndarray):
+        pts = np.ascontiguousarray(scaled_points, dtype=np.float64)
+        self.dim, self.n = pts.shape
+        self.buf = DeviceArray.from_numpy(pts)
+        self._arr = (C.c_void_p * self.dim)(*[self.buf.ptr + 8 * self.n * d for d in range(self.dim)])
+
+    @property
+    def coords(self):
+        return self._arr
+
+
+# ------------------------------------------------------------------- BLAS
+def _s(stream):
+    return None if stream is None else C.c_void_p(int(stream))
+
+
+def dgemv(m, n, A_ptr, lda, x_ptr, y_ptr, stream=None) -> None:
+    check(lib().mgb_dgemv(m, n, A_ptr, lda, x_ptr, y_ptr, _s(stream)))
+
+
+def ddot(n, x_ptr, y_ptr, stream=None) -> float:
+    r = C.c_double()
+    check(lib().mgb_ddot(n, x_ptr, y_ptr, C.byref(r), _s(stream)))
+    return r.value
+
+
+def daxpy(n, alpha, x_ptr, y_ptr, stream=None) -> None:
+    check(lib().mgb_daxpy(n, float(alpha), x_ptr, y_ptr, _s(stream)))
+
+
+def gauss_matvec_f64(pts: GaussPoints, nugget, rule, x_ptr, y_ptr, rows=None, cols=None, row_offset=0,
+                     col_offset=0, stream=None) -> None:
+    rows = pts.n if rows is None else rows
+    cols = pts.n if cols is None else cols
+    check(lib().mgb_gauss_matvec_f64(rows, cols, row_offset, col_offset, pts.dim, pts.coords, float(nugget),
+                                     rule, x_ptr, y_ptr, _s(stream)))
+
+
+def gauss_matvec_mixed(pts: GaussPoints, nugget, x_ptr, y_ptr, stream=None) -> None:
+    check(lib().mgb_gauss_matvec_mixed(pts.n, pts.dim, pts.coords, float(nugget), x_ptr, y_ptr, _s(stream)))
+
+
+def gauss_entries(pts: GaussPoints, i: np.ndarray, j: np.ndarray, nugget=0.0, rule=NUGGET_DIAGONAL) -> np.ndarray:
+    di = DeviceArray.from_numpy(np.asarray(i, dtype=np.int32))
+    dj = DeviceArray.from_numpy(np.asarray(j, dtype=np.int32))
+    out = DeviceArray(len(di.numpy()))
+    check(lib().mgb_gauss_entries_f64(pts.n, di.count, di.ptr, dj.ptr, pts.dim, pts.coords, float(nugget), rule,
+                                      out.ptr, None))
+    return out.numpy()
+
+
+def kernel_launches() -> int:
+    """Kernels launched by the library so far in this process."""
+    return int(lib().mgb_kernel_launches())
+
+
+def time_gauss_matvec(pts: GaussPoints, nugget, precision, x_ptr, y_ptr, reps=10, stream=None) -> float:
+    """Mean milliseconds per launch of the Gaussian matvec kernel (CUDA events)."""
+    ms = C.c_double()
+    check(lib().mgb_time_gauss_matvec(pts.n, pts.dim, pts.coords, float(nugget), precision, x_ptr, y_ptr, reps,
+                                      C.byref(ms), _s(stream)))
+    return ms.value
+
+
+def time_dgemv(n, A_ptr, x_ptr, y_ptr, reps=10, stream=None) -> float:
+    ms = C.c_double()
+    check(lib().mgb_time_dgemv(n, A_ptr, x_ptr, y_ptr, reps, C.byref(ms), _s(stream)))
+    return ms.value
+
+
+# ---------------------------------------------------------------- solvers
+def _solve(status: int, info: SolveInfo, allow_notconv: bool) -> SolveInfo:
+    if status == MGB_ERR_NOTCONV and allow_notconv:
+        return info
+    if status == MGB_ERR_BREAKDOWN and allow_notconv:
+        return info
+    check(status)
+    return info
+
+
+def cg_dense(n, A_ptr, b_ptr, x_ptr, iter_max=1000, eps=1e-10, stop_rule=STOP_RELATIVE, lda=None, stream=None,
+             allow_notconv=True) -> SolveInfo:
+    info = SolveInfo()
+    st = lib().mgb_cg_dense(n, A_ptr, lda or n, b_ptr, x_ptr, iter_max, eps, stop_rule, C.byref(info), _s(stream))
+    return _solve(st, info, allow_notconv)
+
+
+def bicgstab_dense(n, A_ptr, b_ptr, x_ptr, iter_max=1000, eps=1e-10, lda=None, stream=None,
+                   allow_notconv=True) -> SolveInfo:
+    info = SolveInfo()
+    st = lib().mgb_bicgstab_dense(n, A_ptr, lda or n, b_ptr, x_ptr, iter_max, eps, C.byref(info), _s(stream))
+    return _solve(st, info, allow_notconv)
+
+
+def cg_gauss(pts: GaussPoints, nugget, b_ptr, x_ptr, iter_max=100000, eps=1e-10, stop_rule=STOP_RELATIVE,
+             precision=PREC_FP64, rule=NUGGET_DIAGONAL, stream=None, allow_notconv=True) -> SolveInfo:
+    info = SolveInfo()
+    st = lib().mgb_cg_gauss(pts.n, pts.dim, pts.coords, float(nugget), rule, b_ptr, x_ptr, iter_max, eps, stop_rule,
+                            precision, C.byref(info), _s(stream))
+    return _solve(st, info, allow_notconv)
+
+
+def bicgstab_gauss(pts: GaussPoints, nugget, b_ptr, x_ptr, iter_max=100000, eps=1e-10, rule=NUGGET_DIAGONAL,
+                   stream=None, allow_notconv=True) -> SolveInfo:
+    info = SolveInfo()
+    st = lib().mgb_bicgstab_gauss(pts.n, pts.dim, pts.coords, float(nugget), rule, b_ptr, x_ptr, iter_max, eps,
+                                  C.byref(info), _s(stream))
+    return _solve(st, info, allow_notconv)
+
+
+def cg_gauss_host(scaled_points: np.ndarray, nugget: float, b: np.ndarray, x0: np.ndarray | None = None,
+                  iter_max=100000, eps=1e-10, precision=PREC_MIXED, allow_notconv=True):
+    """End-to-end solve from host buffers (points, b, x0 in host memory)."""
+    pts = np.ascontiguousarray(scaled_points, dtype=np.float64)
+    dim, n = pts.shape
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.zeros(n) if x0 is None else np.array(x0, dtype=np.float64, copy=True)
+    info = SolveInfo()
+    st = lib().mgb_cg_gauss_host(n, dim, pts.ctypes.data, float(nugget), b.ctypes.data, x.ctypes.data, iter_max,
+                                 eps, precision, C.byref(info))
+    _solve(st, info, allow_notconv)
+    return x, info

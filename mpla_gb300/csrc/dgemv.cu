@@ -1,0 +1,183 @@
+// Dense FP64 GEMV y = A x for column-major A (the only device compute of
+// mpla_dgemv, MPLA src/mpla.cpp:716-751, which calls cublasDgemv OP_N).
+//
+// HBM-bound: 8 bytes of A per 2 flops.  Layout of the work:
+//   * a CTA owns a strip of 32*VEC rows and a chunk of 8*cpw columns;
+//   * each of its 8 warps streams cpw columns of the strip with 128-bit
+//     (VEC = 2) coalesced, L1-bypassing loads, 8 columns in flight per thread;
+//   * the CTA's slice of x is staged in shared memory by one bulk (TMA) copy;
+//   * warp partials are summed in shared memory in warp order, and chunk
+//     partials across the grid by the last-arriving CTA of each strip in
+//     chunk order — a fixed summation order, so results are bit-reproducible.
+#include "internal.h"
+#include "devutil.cuh"
+
+namespace mgb {
+
+namespace {
+
+constexpr int kWarps = 8;
+constexpr int kThreads = kWarps * 32;
+
+__device__ __forceinline__ double2 ld_stream2(const double* p) {
+  double2 v;
+  asm volatile("ld.global.nc.L1::no_allocate.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "l"(p));
+  return v;
+}
+
+__device__ __forceinline__ double ld_stream1(const double* p) {
+  double v;
+  asm volatile("ld.global.nc.L1::no_allocate.f64 %0, [%1];" : "=d"(v) : "l"(p));
+  return v;
+}
+
+template <int VEC>
+__global__ void __launch_bounds__(kThreads) dgemv_kernel(int m, int n, const double* __restrict__ A,
+                                                         long long lda, const double* __restrict__ x,
+                                                         double* __restrict__ y, int cpw, int nsplit,
+                                                         double* __restrict__ partials,
+                                                         unsigned int* __restrict__ tickets,
+                                                         const int* __restrict__ done,
+                                                         unsigned int* __restrict__ err) {
+  if (done && *done) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  // layout: [mbarrier 16 B][x chunk: 8*cpw doubles][warp partials: 8 x 32*VEC doubles]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+  double* xs = reinterpret_cast<double*>(smem_raw + 16);
+  const int chunk = kWarps * cpw;
+  double* wpart = xs + chunk;
+  __shared__ int s_last;
+
+  constexpr int kRows = 32 * VEC;
+  const int strip = blockIdx.x / nsplit;
+  const int split = blockIdx.x % nsplit;
+  const int row0 = strip * kRows;
+  const int col0 = split * chunk;
+  const int ncols = min(chunk, n - col0);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+
+  // ---- stage x[col0 : col0+ncols) in shared memory
+  const bool use_bulk = ((reinterpret_cast<uintptr_t>(x + col0) & 15) == 0) && ((ncols & 1) == 0);
+  if (use_bulk) {
+    if (threadIdx.x == 0) {
+      mbar_init(bar, 1);
+      fence_proxy_async_smem();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      mbar_arrive_expect_tx(bar, ncols * 8);
+      bulk_copy_g2s(xs, x + col0, ncols * 8, bar);
+    }
+  } else {
+    for (int j = threadIdx.x; j < ncols; j += kThreads) xs[j] = x[col0 + j];
+  }
+
+  // ---- stream A: this warp's columns [wc0, wc1) of the chunk
+  const int wc0 = warp * cpw;
+  const int wc1 = min(wc0 + cpw, ncols);
+  const int r = row0 + lane * VEC;
+  double acc0 = 0.0, acc1 = 0.0;
+  bool x_ready = true;
+  if (use_bulk) x_ready = mbar_wait_bounded(bar, 0, err, DEV_ERR_WAIT_TIMEOUT);
+  if (x_ready && r < m && wc0 < wc1) {
+    const double* a = A + (long long)(col0 + wc0) * lda + r;
+    const bool pair = (VEC == 2) && (r + 1 < m);
+    int j = wc0;
+    for (; j + 8 <= wc1; j += 8) {
+      if (VEC == 2 && pair) {
+        double2 v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = ld_stream2(a + (long long)u * lda);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const double xv = xs[j + u];
+          acc0 = fma(v[u].x, xv, acc0);
+          acc1 = fma(v[u].y, xv, acc1);
+        }
+      } else {
+        double v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = ld_stream1(a + (long long)u * lda);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) acc0 = fma(v[u], xs[j + u], acc0);
+      }
+      a += 8 * lda;
+    }
+    for (; j < wc1; ++j) {
+      const double xv = xs[j];
+      if (VEC == 2 && pair) {
+        const double2 v = ld_stream2(a);
+        acc0 = fma(v.x, xv, acc0);
+        acc1 = fma(v.y, xv, acc1);
+      } else {
+        acc0 = fma(ld_stream1(a), xv, acc0);
+      }
+      a += lda;
+    }
+  }
+  wpart[warp * kRows + lane * VEC] = acc0;
+  if (VEC == 2) wpart[warp * kRows + lane * VEC + 1] = acc1;
+  __syncthreads();
+
+  // ---- CTA partial for the strip: sum warps in order
+  double cta_sum = 0.0;
+  const int lr = threadIdx.x;
+  if (lr < kRows) {
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) cta_sum += wpart[w * kRows + lr];
+  }
+  if (nsplit == 1) {
+    if (lr < kRows && row0 + lr < m) y[row0 + lr] = cta_sum;
+    return;
+  }
+  if (lr < kRows && row0 + lr < m) partials[(long long)split * m + row0 + lr] = cta_sum;
+  if (last_block_arrival(&tickets[strip], nsplit, &s_last)) {
+    if (lr < kRows && row0 + lr < m) {
+      double s = 0.0;
+#pragma unroll 8
+      for (int q = 0; q < nsplit; ++q) s += __ldcg(&partials[(long long)q * m + row0 + lr]);
+      y[row0 + lr] = s;
+    }
+  }
+}
+
+}  // namespace
+
+int launch_dgemv(DeviceContext* c, int m, int n, const double* A, int lda, const double* x,
+                 double* y, cudaStream_t s, const int* done) {
+  if (m < 0 || n < 0 || lda < (m > 1 ? m : 1))
+    return set_error(MGB_ERR_ARG, "dgemv: bad sizes m=%d n=%d lda=%d", m, n, lda);
+  if (m == 0) return MGB_OK;
+  if (n == 0) {
+    MGB_CUDA(cudaMemsetAsync(y, 0, sizeof(double) * m, s));
+    return MGB_OK;
+  }
+  const bool vec2 = ((lda & 1) == 0) && ((reinterpret_cast<uintptr_t>(A) & 15) == 0);
+  const int rows_per_strip = vec2 ? 64 : 32;
+  const int strips = (m + rows_per_strip - 1) / rows_per_strip;
+  // Columns per warp: enough CTAs to cover the machine several times over,
+  // at least 16 columns per warp so each thread keeps 8 loads in flight.
+  int cpw = 128;
+  const long long target = 6LL * c->num_sms;
+  while (cpw > 16 && (long long)strips * ((n + kWarps * cpw - 1) / (kWarps * cpw)) < target) cpw >>= 1;
+  const int nsplit = (n + kWarps * cpw - 1) / (kWarps * cpw);
+  if (nsplit > 1) {
+    MGB_TRY(ensure_split_partials(c, (size_t)nsplit * m));
+    MGB_TRY(ensure_tickets(c, strips + 1));
+  }
+  const size_t smem = 16 + sizeof(double) * (kWarps * cpw + kWarps * rows_per_strip);
+  const long long grid = (long long)strips * nsplit;
+  if (grid > 0x7fffffffLL) return set_error(MGB_ERR_ARG, "dgemv: grid too large");
+  if (vec2) {
+    dgemv_kernel<2><<<(unsigned)grid, kThreads, smem, s>>>(m, n, A, lda, x, y, cpw, nsplit,
+                                                         c->split_partials, c->tickets + 1, done, c->dev_error);
+  } else {
+    dgemv_kernel<1><<<(unsigned)grid, kThreads, smem, s>>>(m, n, A, lda, x, y, cpw, nsplit,
+                                                         c->split_partials, c->tickets + 1, done, c->dev_error);
+  }
+  count_launches(1);
+  MGB_CUDA(cudaGetLastError());
+  return MGB_OK;
+}
+
+}  // namespace mgb

@@ -1,0 +1,64 @@
+// Matvec adapters used by the solver drivers and the mpla.h cores.
+#pragma once
+
+#include "internal.h"
+
+namespace mgb {
+
+// Scaled copy of a Gaussian system's coordinates (gauss_f64.cu).
+struct ScaledCoords {
+  double* buf = nullptr;
+  const double* ptr[3] = {nullptr, nullptr, nullptr};
+  const double* const* dev_ptrs = nullptr;
+};
+int prepare_scaled_coords(DeviceContext* c, const GaussSystem& g, ScaledCoords* out, cudaStream_t s);
+void release_scaled_coords(DeviceContext* c, ScaledCoords* sc);
+int launch_gauss_f64_scaled(DeviceContext* c, const GaussSystem& g, const double* const* scaled,
+                            const double* const* scaled_dev_ptrs, const double* x, double* y,
+                            cudaStream_t s, const int* skip);
+int make_gauss_system(int n, int dim, const double* const* coords, double nugget, int rule, GaussSystem* g);
+
+// Dense column-major matrix through the library's dgemv.
+class DenseMatvec : public Matvec {
+ public:
+  DenseMatvec(DeviceContext* c, int n, const double* A, int lda) : c_(c), n_(n), A_(A), lda_(lda) {}
+  int apply(const double* x, double* y, cudaStream_t s, const int* skip) override;
+  int n() const override { return n_; }
+
+ private:
+  DeviceContext* c_;
+  int n_;
+  const double* A_;
+  int lda_;
+};
+
+// Gaussian kernel matrix, FP64 fused matvec (coordinates scaled once).
+class GaussF64Matvec : public Matvec {
+ public:
+  ~GaussF64Matvec() override;
+  int init(DeviceContext* c, const GaussSystem& g, cudaStream_t s);
+  int apply(const double* x, double* y, cudaStream_t s, const int* skip) override;
+  int n() const override { return g_.rows; }
+
+ private:
+  DeviceContext* c_ = nullptr;
+  GaussSystem g_{};
+  ScaledCoords sc_;
+};
+
+// Gaussian kernel matrix, FP32/SFU matvec (square systems).
+struct MixedSystem;
+class GaussMixedMatvec : public Matvec {
+ public:
+  ~GaussMixedMatvec() override;
+  int init(DeviceContext* c, const GaussSystem& g, cudaStream_t s);
+  int apply(const double* x, double* y, cudaStream_t s, const int* skip) override;
+  int n() const override { return n_; }
+
+ private:
+  DeviceContext* c_ = nullptr;
+  MixedSystem* m_ = nullptr;
+  int n_ = 0;
+};
+
+}  // namespace mgb

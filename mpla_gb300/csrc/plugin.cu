@@ -1,0 +1,307 @@
+// The plugin interfaces of MPLA on GB300: the kernel.h cores (host
+// descriptor, kernel.cu nugget rule), the generic system_assembler adapter,
+// the Gaussian assembler factory, and the right-hand-side generators.
+//
+// The reference materialises row blocks of K and calls cublasDgemv on them
+// (kernel.cu:87-171, generic_system_adapter.cu:53-137).  Here:
+//   * Gaussian systems — from a kernel_matrix_data descriptor or from an
+//     assembler made by this library's factory — run the fused FP64 kernel
+//     (no matrix storage, so max_row_count_per_dgemv has nothing to bound);
+//   * any other system_assembler runs a fused kernel that calls its virtual
+//     get_matrix_entry per entry, again without storing the matrix.
+#include <cstring>
+#include <mutex>
+#include <set>
+
+#include "../../include/mpla.h"
+#include "../../include/kernel.h"
+#include "../../include/generic_system_adapter.h"
+#include "../../include/kernel_system_assembler.h"
+#include "internal.h"
+#include "devutil.cuh"
+#include "matvecs.h"
+#include "plugin.h"
+
+namespace mgb {
+
+namespace {
+
+std::mutex g_registry_mutex;
+std::set<const void*> g_gauss_objects;  // device objects created by our factory
+
+void die(int st) {
+  if (st != MGB_OK) {
+    fprintf(stderr, "MPLA: %s\n", mgb_last_error());
+    exit(EXIT_FAILURE);
+  }
+}
+
+DeviceContext* ctx() {
+  DeviceContext* c = nullptr;
+  die(context(&c));
+  return c;
+}
+
+__global__ void k_create_gauss(gaussian_kernel_system_assembler** out, double** points, int max_rows, int dim,
+                               double regularization) {
+  gaussian_kernel_system_assembler* a = new gaussian_kernel_system_assembler();
+  if (a) {
+    a->points = points;
+    a->max_row_count_per_dgemv = max_rows;
+    a->dim = dim;
+    a->regularization = regularization;
+  }
+  *out = a;
+}
+
+__global__ void k_destroy_gauss(gaussian_kernel_system_assembler** obj) {
+  delete *obj;
+  *obj = nullptr;
+}
+
+// Generic fused matvec: one row per thread, a column range per CTA, entries
+// from the object's virtual get_matrix_entry; x staged in shared memory.
+constexpr int kGenThreads = 128;
+constexpr int kGenTileJ = 256;
+
+__global__ void __launch_bounds__(kGenThreads) k_generic_matvec(system_assembler* assem, int rows, int cols,
+                                                                int row_offset, int col_offset,
+                                                                const double* __restrict__ x, double* __restrict__ y,
+                                                                int cols_per_split, int nsplit,
+                                                                double* __restrict__ partials,
+                                                                unsigned int* __restrict__ tickets,
+                                                                const int* __restrict__ skip) {
+  if (skip && *skip) return;
+  __shared__ double sx[kGenTileJ];
+  __shared__ int s_last;
+  const int tile = blockIdx.x / nsplit, split = blockIdx.x % nsplit;
+  const int i = tile * kGenThreads + threadIdx.x;
+  const int cbeg = split * cols_per_split, cend = min(cols, cbeg + cols_per_split);
+  double acc = 0.0;
+  for (int j0 = cbeg; j0 < cend; j0 += kGenTileJ) {
+    const int nj = min(kGenTileJ, cend - j0);
+    __syncthreads();
+    for (int t = threadIdx.x; t < nj; t += kGenThreads) sx[t] = x[j0 + t];
+    __syncthreads();
+    if (i < rows)
+      for (int t = 0; t < nj; ++t) acc = fma(assem->get_matrix_entry(row_offset + i, col_offset + j0 + t), sx[t], acc);
+  }
+  if (nsplit == 1) {
+    if (i < rows) y[i] = acc;
+    return;
+  }
+  if (i < rows) partials[(long long)split * rows + i] = acc;
+  if (last_block_arrival(&tickets[tile], nsplit, &s_last)) {
+    if (i < rows) {
+      double s = 0.0;
+      for (int p = 0; p < nsplit; ++p) s += __ldcg(&partials[(long long)p * rows + i]);
+      y[i] = s;
+    }
+  }
+}
+
+__global__ void k_generic_rhs(system_assembler* assem, int rows, int row_offset, double* __restrict__ b) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < rows) b[i] = assem->get_rhs_entry(row_offset + i);
+}
+
+// rhs_i = prod_d (sqrt(pi)/2) (erf(1 - p_d[i]) - erf(-p_d[i]))   (kernel.cu:52-68)
+__global__ void k_gauss_rhs(const double* const* __restrict__ points, int dim, int rows, int row_offset,
+                            double* __restrict__ b) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= rows) return;
+  const double half_sqrt_pi = 0.88622692545275801365;
+  double prod = 1.0;
+  for (int d = 0; d < dim; ++d) {
+    const double p = points[d][row_offset + i];
+    prod = prod * half_sqrt_pi * (erf(1.0 - p) - erf(0.0 - p));
+  }
+  b[i] = prod;
+}
+
+class GenericAssemblerMatvec : public Matvec {
+ public:
+  GenericAssemblerMatvec(DeviceContext* c, mpla_generic_matrix* A) : c_(c), A_(A) {}
+  int apply(const double* x, double* y, cudaStream_t s, const int* skip) override {
+    const int rows = A_->cur_proc_row_count, cols = A_->cur_proc_col_count;
+    if (rows <= 0) return MGB_OK;
+    const int tiles = (rows + kGenThreads - 1) / kGenThreads;
+    int nsplit = (8 * c_->num_sms + tiles - 1) / tiles;
+    nsplit = max(1, min(nsplit, (cols + 255) / 256));
+    const int cps = (cols + nsplit - 1) / nsplit;
+    nsplit = (cols + cps - 1) / cps;
+    if (nsplit > 1) {
+      MGB_TRY(ensure_split_partials(c_, (size_t)nsplit * rows));
+      MGB_TRY(ensure_tickets(c_, tiles + 1));
+    }
+    k_generic_matvec<<<tiles * nsplit, kGenThreads, 0, s>>>(static_cast<system_assembler*>(A_->data), rows, cols,
+                                                            A_->cur_proc_row_offset, A_->cur_proc_col_offset, x, y,
+                                                            cps, nsplit, c_->split_partials, c_->tickets + 1, skip); count_launches(1);
+    MGB_CUDA(cudaGetLastError());
+    return MGB_OK;
+  }
+  int n() const override { return A_->cur_proc_row_count; }
+
+ private:
+  DeviceContext* c_;
+  mpla_generic_matrix* A_;
+};
+
+}  // namespace
+
+int kernel_data_system(const kernel_matrix_data* kd, const mpla_generic_matrix* A, GaussSystem* g) {
+  if (!kd || !kd->points) return set_error(MGB_ERR_ARG, "kernel_matrix_data without points");
+  if (kd->dim < 1 || kd->dim > kMaxGaussDim)
+    return set_error(MGB_ERR_ARG, "kernel_matrix_data.dim = %d not in [1,%d]", kd->dim, kMaxGaussDim);
+  memset(g, 0, sizeof(*g));
+  g->dim = kd->dim;
+  MGB_CUDA(cudaMemcpy(g->coords, kd->points, sizeof(double*) * kd->dim, cudaMemcpyDeviceToHost));
+  g->rows = A->cur_proc_row_count;
+  g->cols = A->cur_proc_col_count;
+  g->row_offset = A->cur_proc_row_offset;
+  g->col_offset = A->cur_proc_col_offset;
+  g->nugget = 1e-8;
+  g->nugget_rule = MGB_NUGGET_KERNEL_CU;
+  return MGB_OK;
+}
+
+int assembler_system(const void* obj, const mpla_generic_matrix* A, GaussSystem* g) {
+  {
+    std::lock_guard<std::mutex> lock(g_registry_mutex);
+    if (!obj || !g_gauss_objects.count(obj)) return set_error(MGB_ERR_ARG, "not a library Gaussian assembler");
+  }
+  // Field values are read from the device object on every call, so a caller
+  // that patches points or regularization in place is honoured.
+  alignas(16) unsigned char raw[sizeof(gaussian_kernel_system_assembler)];
+  MGB_CUDA(cudaMemcpy(raw, obj, sizeof(raw), cudaMemcpyDeviceToHost));
+  const gaussian_kernel_system_assembler* h = reinterpret_cast<const gaussian_kernel_system_assembler*>(raw);
+  if (h->dim < 1 || h->dim > kMaxGaussDim)
+    return set_error(MGB_ERR_ARG, "assembler dim %d not in [1,%d]", h->dim, kMaxGaussDim);
+  memset(g, 0, sizeof(*g));
+  g->dim = h->dim;
+  MGB_CUDA(cudaMemcpy(g->coords, h->points, sizeof(double*) * h->dim, cudaMemcpyDeviceToHost));
+  g->rows = A->cur_proc_row_count;
+  g->cols = A->cur_proc_col_count;
+  g->row_offset = A->cur_proc_row_offset;
+  g->col_offset = A->cur_proc_col_offset;
+  g->nugget = h->regularization;
+  g->nugget_rule = MGB_NUGGET_DIAGONAL;
+  return MGB_OK;
+}
+
+Matvec* new_generic_assembler_matvec(DeviceContext* c, mpla_generic_matrix* A) {
+  return new GenericAssemblerMatvec(c, A);
+}
+
+}  // namespace mgb
+
+using namespace mgb;
+
+// --------------------------------------------------------- kernel.h cores
+void mpla_set_gaussian_kernel_rhs(struct mpla_vector* b, struct mpla_generic_matrix* A, struct mpla_instance* instance) {
+  (void)instance;
+  DeviceContext* c = ctx();
+  const kernel_matrix_data* kd = static_cast<const kernel_matrix_data*>(A->data);
+  const int rows = A->cur_proc_row_count;
+  k_gauss_rhs<<<(rows + 255) / 256, 256, 0, c->stream>>>(kd->points, kd->dim, rows, A->cur_proc_row_offset, b->data); count_launches(1);
+  cudaStreamSynchronize(c->stream);
+  checkCUDAError("gen_gaussian_kernel_rhs");
+}
+
+static void gauss_core_kernel_data(struct mpla_vector* b, struct mpla_generic_matrix* A, struct mpla_vector* x) {
+  DeviceContext* c = ctx();
+  GaussSystem g;
+  die(kernel_data_system(static_cast<const kernel_matrix_data*>(A->data), A, &g));
+  die(launch_gauss_f64(c, g, x->data, b->data, c->stream, nullptr));
+}
+
+void mpla_dgemv_core_kernel_cublas(struct mpla_vector* b, struct mpla_generic_matrix* A, struct mpla_vector* x_redist,
+                                   struct mpla_instance* instance) {
+  (void)instance;
+  gauss_core_kernel_data(b, A, x_redist);
+}
+
+void mpla_dgemv_core_kernel_streamed_cublas(struct mpla_vector* b, struct mpla_generic_matrix* A,
+                                            struct mpla_vector* x_redist, struct mpla_instance* instance) {
+  (void)instance;
+  gauss_core_kernel_data(b, A, x_redist);
+}
+
+void mpla_dgemv_core_dense(struct mpla_vector* b, struct mpla_generic_matrix* A, struct mpla_vector* x_redist,
+                           struct mpla_instance* instance) {
+  (void)instance;
+  DeviceContext* c = ctx();
+  die(launch_dgemv(c, A->cur_proc_row_count, A->cur_proc_col_count, static_cast<const double*>(A->data),
+                   A->cur_proc_row_count, x_redist->data, b->data, c->stream, nullptr));
+}
+
+// ------------------------------------------- generic_system_adapter.h cores
+static void generic_core(struct mpla_vector* b, struct mpla_generic_matrix* A, struct mpla_vector* x) {
+  DeviceContext* c = ctx();
+  GaussSystem g;
+  if (assembler_system(A->data, A, &g) == MGB_OK) {
+    die(launch_gauss_f64(c, g, x->data, b->data, c->stream, nullptr));
+    return;
+  }
+  GenericAssemblerMatvec M(c, A);
+  die(M.apply(x->data, b->data, c->stream, nullptr));
+}
+
+void mpla_dgemv_core_generic_system_matrix_cublas(struct mpla_vector* b, struct mpla_generic_matrix* A,
+                                                  struct mpla_vector* x_redist, struct mpla_instance* instance) {
+  (void)instance;
+  generic_core(b, A, x_redist);
+}
+
+void mpla_dgemv_core_generic_system_matrix_streamed_cublas(struct mpla_vector* b, struct mpla_generic_matrix* A,
+                                                           struct mpla_vector* x_redist, struct mpla_instance* instance) {
+  (void)instance;
+  generic_core(b, A, x_redist);
+}
+
+void mpla_set_generic_system_rhs(struct mpla_vector* b, struct mpla_generic_matrix* A, struct mpla_instance* instance) {
+  (void)instance;
+  DeviceContext* c = ctx();
+  const int rows = A->cur_proc_row_count;
+  k_generic_rhs<<<(rows + 255) / 256, 256, 0, c->stream>>>(static_cast<system_assembler*>(A->data), rows,
+                                                          A->cur_proc_row_offset, b->data); count_launches(1);
+  cudaStreamSynchronize(c->stream);
+  checkCUDAError("gen_generic_system_rhs");
+}
+
+// ------------------------------------------ kernel_system_assembler.h factory
+void create_gaussian_kernel_system_assembler_object_with_regularization(struct gaussian_kernel_system_assembler** assem,
+                                                                       double** points, int max_row_count_per_dgemv,
+                                                                       int dim, double regularization) {
+  DeviceContext* c = ctx();
+  k_create_gauss<<<1, 1, 0, c->stream>>>(assem, points, max_row_count_per_dgemv, dim, regularization); count_launches(1);
+  cudaStreamSynchronize(c->stream);
+  checkCUDAError("create_gaussian_kernel_system_assembler_object");
+  gaussian_kernel_system_assembler* obj = nullptr;
+  cudaMemcpy(&obj, assem, sizeof(obj), cudaMemcpyDeviceToHost);
+  checkCUDAError("create_gaussian_kernel_system_assembler_object");
+  if (!obj) {
+    fprintf(stderr, "MPLA: device heap exhausted creating the assembler\n");
+    exit(EXIT_FAILURE);
+  }
+  std::lock_guard<std::mutex> lock(g_registry_mutex);
+  g_gauss_objects.insert(obj);
+}
+
+void create_gaussian_kernel_system_assembler_object(struct gaussian_kernel_system_assembler** assem, double** points,
+                                                    int max_row_count_per_dgemv, int dim) {
+  create_gaussian_kernel_system_assembler_object_with_regularization(assem, points, max_row_count_per_dgemv, dim, 0.0);
+}
+
+void destroy_gaussian_kernel_system_assembler_object(struct gaussian_kernel_system_assembler** assem) {
+  DeviceContext* c = ctx();
+  gaussian_kernel_system_assembler* obj = nullptr;
+  cudaMemcpy(&obj, assem, sizeof(obj), cudaMemcpyDeviceToHost);
+  {
+    std::lock_guard<std::mutex> lock(g_registry_mutex);
+    g_gauss_objects.erase(obj);
+  }
+  k_destroy_gauss<<<1, 1, 0, c->stream>>>(assem); count_launches(1);
+  cudaStreamSynchronize(c->stream);
+  checkCUDAError("destroy_gaussian_kernel_system_assembler_object");
+}
