@@ -5,6 +5,7 @@
 
 #include "internal.h"
 #include "matvecs.h"
+#include "gauss_sym.h"
 
 namespace mgb {
 
@@ -12,28 +13,43 @@ int DenseMatvec::apply(const double* x, double* y, cudaStream_t s, const int* sk
   return launch_dgemv(c_, n_, n_, A_, lda_, x, y, s, skip);
 }
 
-GaussF64Matvec::~GaussF64Matvec() { release_scaled_coords(c_, &sc_); }
+static bool symmetric_ok(const GaussSystem& g) {
+  return g.rows == g.cols && g.row_offset == 0 && g.col_offset == 0 && g.dim >= 1 && g.dim <= 3 &&
+         g.nugget_rule == MGB_NUGGET_DIAGONAL;
+}
+
+GaussF64Matvec::~GaussF64Matvec() {
+  delete sym_;
+  if (c_) release_scaled_coords(c_, &sc_);
+}
 
 int GaussF64Matvec::init(DeviceContext* c, const GaussSystem& g, cudaStream_t s) {
-  c_ = c;
   g_ = g;
+  if (symmetric_ok(g)) {
+    SymF64* m = new SymF64();
+    sym_ = m;
+    return m->init(c, g);
+  }
+  c_ = c;
   return prepare_scaled_coords(c, g, &sc_, s);
 }
 
 int GaussF64Matvec::apply(const double* x, double* y, cudaStream_t s, const int* skip) {
+  if (sym_) return sym_->apply(x, y, s, skip);
   return launch_gauss_f64_scaled(c_, g_, sc_.ptr, sc_.dev_ptrs, x, y, s, skip);
 }
 
-GaussMixedMatvec::~GaussMixedMatvec() { mixed_release(c_, m_); }
+GaussMixedMatvec::~GaussMixedMatvec() { delete impl_; }
 
 int GaussMixedMatvec::init(DeviceContext* c, const GaussSystem& g, cudaStream_t s) {
-  c_ = c;
   n_ = g.rows;
-  return mixed_prepare(c, g, &m_, s);
+  SymF32* m = new SymF32();
+  impl_ = m;
+  return m->init(c, g, s);
 }
 
 int GaussMixedMatvec::apply(const double* x, double* y, cudaStream_t s, const int* skip) {
-  return launch_gauss_mixed(c_, m_, x, y, s, skip);
+  return impl_->apply(x, y, s, skip);
 }
 
 int make_gauss_system(int n, int dim, const double* const* coords, double nugget, int rule, GaussSystem* g) {
@@ -134,6 +150,13 @@ int mgb_gauss_matvec_f64(int rows, int cols, int row_offset, int col_offset, int
     MGB_CUDA(cudaMemsetAsync(y, 0, sizeof(double) * rows, s));
     return MGB_OK;
   }
+  if (symmetric_ok(g)) {
+    GaussF64Matvec A;
+    MGB_TRY(A.init(c, g, s));
+    MGB_TRY(A.apply(x, y, s, nullptr));
+    MGB_CUDA(cudaStreamSynchronize(s));  // the pool block of A is released on return
+    return MGB_OK;
+  }
   return launch_gauss_f64(c, g, x, y, s, nullptr);
 }
 
@@ -146,7 +169,7 @@ int mgb_gauss_matvec_mixed(int n, int dim, const double* const* coords, double n
   GaussMixedMatvec A;
   MGB_TRY(A.init(c, g, s));
   MGB_TRY(A.apply(x, y, s, nullptr));
-  MGB_CUDA(cudaStreamSynchronize(s));
+  MGB_CUDA(cudaStreamSynchronize(s));  // the pool blocks of A are released on return
   return MGB_OK;
 }
 

@@ -70,6 +70,7 @@ __global__ void __launch_bounds__(kThreads) dgemv_kernel(int m, int n, const dou
     }
   } else {
     for (int j = threadIdx.x; j < ncols; j += kThreads) xs[j] = x[col0 + j];
+    __syncthreads();
   }
 
   // ---- stream A: this warp's columns [wc0, wc1) of the chunk

@@ -1,4 +1,6 @@
-// Matrix-free FP64 Gaussian kernel matvec y = K x.
+// Matrix-free FP64 Gaussian kernel matvec y = K x over a rectangular block
+// (rows x cols with offsets; square systems use the symmetric tile-pair
+// kernel of gauss_sym.cu, which evaluates each entry pair once).
 //
 // Replaces the reference's three-pass core (gen_dis_matrix -> apply_kernel ->
 // cublasDgemv, MPLA src/kernel.cu:17-50,118-171, and the virtual-call
@@ -7,14 +9,15 @@
 //
 // On GB300 the FP64 pipe (about 2 FMA/clk/SM) is the bound, so the kernel
 // minimises FP64 instructions per entry:
-//   * points are pre-scaled by sqrt(4096/ln2) once per call, so the squared
-//     distance is directly the argument t of the table exponential;
+//   * distances come from the caller's coordinates (one rounding per
+//     difference, as in the reference) and are scaled once into the argument
+//     t of the table exponential;
 //   * exp(-s) uses the 4096-entry table method (devutil.cuh): round, a
 //     degree-3 polynomial and one FMA, with the power of two and the range
 //     checks done on the integer pipe;
 //   * the diagonal nugget is added once per row after the loop instead of
 //     being tested on every entry.
-// 2 + 2*DIM + 8 FP64 operations per entry (12 for d = 2).
+// 3 + 2*DIM + 8 FP64 operations per entry (13 for d = 2).
 //
 // Work layout: a CTA owns 256 rows (128 threads x 2 rows in registers) and a
 // column range; source tiles of 128 points (coordinates + x values) and the
@@ -127,9 +130,10 @@ __global__ void __launch_bounds__(kThreads) gauss_f64_kernel(
             s = (d == 0) ? df * df : fma(df, df, s);
           }
         }
-        double e = exp_neg_scaled(s, table);
+        const double ts = s * kExpScale;
+        double e = exp_neg_scaled(ts, table);
         if (RULE == MGB_NUGGET_KERNEL_CU) {
-          if (below_kernel_cu_tiny(s)) e += 1e-8;
+          if (below_kernel_cu_tiny(ts)) e += 1e-8;
         }
         acc[q] = fma(e, xv, acc[q]);
       }
@@ -190,9 +194,10 @@ __global__ void gauss_entries_kernel(int count, const int* __restrict__ ii, cons
     const double df = coords[0][(long long)d * stride + i] - coords[0][(long long)d * stride + j];
     s = (d == 0) ? df * df : fma(df, df, s);
   }
-  double e = exp_neg_scaled(s, table);
+  const double ts = s * kExpScale;
+  double e = exp_neg_scaled(ts, table);
   if (rule == MGB_NUGGET_KERNEL_CU) {
-    if (below_kernel_cu_tiny(s)) e += 1e-8;
+    if (below_kernel_cu_tiny(ts)) e += 1e-8;
   } else if (i == j) {
     e += nugget;
   }
@@ -213,7 +218,7 @@ static int make_scaled_coords(DeviceContext* c, const GaussSystem& g, double** o
   const double* host_ptrs[kMaxDim];
   for (int d = 0; d < g.dim; ++d) host_ptrs[d] = g.coords[d];
   MGB_CUDA(cudaMemcpyAsync(ptrs, host_ptrs, sizeof(double*) * g.dim, cudaMemcpyHostToDevice, s));
-  const double f = sqrt(kExpScale);
+  const double f = 1.0;  // plain copy: distances are formed from the caller's coordinates
   const long long total = (long long)n * g.dim;
   const long long want = (total + 255) / 256, cap = 4LL * c->num_sms;
   const int blocks = (int)(want < cap ? want : cap);

@@ -1,0 +1,415 @@
+// Symmetric tile-pair Gaussian matvec y = K x for square systems, in FP64
+// (plain CG) and FP32 (mixed CG).
+//
+// K is symmetric, so each 128 x 128 tile pair (I, J) with I <= J is
+// evaluated once and used twice: its row sums go to tile I and, for I < J,
+// its column sums go to tile J.  That halves the exponentials per matvec
+// compared with the reference, which builds and multiplies every entry
+// (MPLA src/kernel.cu:118-171, src/generic_system_adapter.cu:83-137).
+//
+//   pair kernel   one CTA per tile pair; 256 threads in a 16 x 16 grid, each
+//                 thread an 8 x 8 register block of entries, with row and
+//                 column accumulators in registers.  Row sums reduce across
+//                 a half-warp with shuffles, column sums across the CTA in
+//                 shared memory.  Each contribution is written to its own
+//                 slot S[tile][other tile][row]: no atomics.
+//   reduce kernel y_i = sum over the T slots of row i in tile order (FP64),
+//                 + nugget x_i: a fixed order, so the product is
+//                 bit-reproducible.
+//
+// FP64: entries exp(-s) with the table exponential (devutil.cuh) on the
+// squared distance of the caller's coordinates; 15 FP64 operations per
+// evaluated entry, 7.5 per matrix entry (d = 2).
+// FP32: points are Morton-ordered and stored relative to the centre of their
+// tile, and each tile pair adds the difference of the two centres (computed
+// in FP64) once per row, so distances keep FP32 relative accuracy however far
+// the points are from the origin; exponentials on the SFU (ex2.approx, with
+// coordinates pre-scaled by sqrt(log2 e)).  7 issue slots and 1 MUFU per
+// evaluated entry, i.e. 0.5 MUFU per matrix entry.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "internal.h"
+#include "devutil.cuh"
+#include "matvecs.h"
+#include "gauss_sym.h"
+
+namespace mgb {
+
+namespace {
+
+constexpr int kB = 128;        // tile edge
+constexpr int kThreads = 256;  // 16 x 16
+constexpr int kR = 8;          // rows per thread
+constexpr int kC = 8;          // columns per thread
+
+__device__ __forceinline__ float ex2_approx(float v) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(v));
+  return r;
+}
+
+// tile pair index p -> (I, J), I <= J, enumerating the upper triangle row by
+// row: p = I*T - I*(I-1)/2 + (J - I).
+__device__ __forceinline__ void pair_of(long long p, int T, int* I, int* J) {
+  // I = largest i with start(i) <= p, start(i) = i*T - i*(i-1)/2
+  const double tt = 2.0 * T + 1.0;
+  int i = (int)floor((tt - sqrt(tt * tt - 8.0 * (double)p)) * 0.5);
+  if (i < 0) i = 0;
+  if (i > T - 1) i = T - 1;
+  auto start = [&](long long k) { return k * T - k * (k - 1) / 2; };
+  while (i > 0 && start(i) > p) --i;
+  while (i + 1 < T && start(i + 1) <= p) ++i;
+  *I = i;
+  *J = i + (int)(p - start(i));
+}
+
+// Write the CTA's row sums (acc_r, one per thread row) and column sums.
+template <typename AccT>
+__device__ __forceinline__ void store_sums(AccT (&acc_r)[kR], AccT (&acc_c)[kC], AccT* slot_row, AccT* slot_col,
+                                           AccT* colbuf, int ty, int tx) {
+  // rows: reduce across the 16 lanes that share ty (a half-warp)
+#pragma unroll
+  for (int a = 0; a < kR; ++a) {
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) acc_r[a] += __shfl_xor_sync(0xffffffffu, acc_r[a], o, 16);
+  }
+  if (tx < kR) {
+    AccT v = acc_r[0];
+#pragma unroll
+    for (int a = 1; a < kR; ++a)
+      if (tx == a) v = acc_r[a];
+    slot_row[ty + 16 * tx] = v;
+  }
+  if (slot_col) {
+    // columns: 16 partial sums per column (one per ty), summed in ty order;
+    // colbuf may alias data the other threads were still reading
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < kC; ++b) colbuf[ty * kB + tx + 16 * b] = acc_c[b];
+    __syncthreads();
+    if (threadIdx.x < kB) {
+      AccT v = 0;
+#pragma unroll
+      for (int q = 0; q < 16; ++q) v += colbuf[q * kB + threadIdx.x];
+      slot_col[threadIdx.x] = v;
+    }
+  }
+}
+
+// ----------------------------------------------------------------- FP64
+template <int DIM>
+__global__ void __launch_bounds__(kThreads) sym_f64_pair_kernel(int n, int T, const double* __restrict__ c0,
+                                                                const double* __restrict__ c1,
+                                                                const double* __restrict__ c2,
+                                                                const double* __restrict__ x,
+                                                                const double* __restrict__ table_g,
+                                                                double* __restrict__ S, const int* __restrict__ skip) {
+  if (skip && *skip) return;
+  // the exp table is dead once the entries are evaluated; the column
+  // reduction buffer (16 x 128 doubles) reuses its storage
+  __shared__ double table[kExpTableSize];
+  __shared__ double sp[2][DIM][kB];
+  __shared__ double sxv[2][kB];
+  double* colbuf = table;
+  static_assert(16 * kB <= kExpTableSize, "column buffer must fit in the table storage");
+  int I, J;
+  pair_of(blockIdx.x, T, &I, &J);
+  for (int i = threadIdx.x; i < kExpTableSize; i += kThreads) table[i] = table_g[i];
+  for (int t = threadIdx.x; t < 2 * kB; t += kThreads) {
+    const int side = t / kB, k = t % kB;
+    const int g = (side ? J : I) * kB + k;
+    const bool in = g < n;
+    const int gc = in ? g : n - 1;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) sp[side][d][k] = (d == 0 ? c0 : (d == 1 ? c1 : c2))[gc];
+    sxv[side][k] = in ? x[g] : 0.0;
+  }
+  __syncthreads();
+  const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
+  double ri[kR][DIM], xi[kR];
+#pragma unroll
+  for (int a = 0; a < kR; ++a) {
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) ri[a][d] = sp[0][d][ty + 16 * a];
+    xi[a] = sxv[0][ty + 16 * a];
+  }
+  double acc_r[kR], acc_c[kC];
+#pragma unroll
+  for (int a = 0; a < kR; ++a) acc_r[a] = 0.0;
+#pragma unroll
+  for (int b = 0; b < kC; ++b) acc_c[b] = 0.0;
+  const bool diag = (I == J);
+#pragma unroll
+  for (int b = 0; b < kC; ++b) {
+    double cj[DIM];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) cj[d] = sp[1][d][tx + 16 * b];
+    const double xj = sxv[1][tx + 16 * b];
+#pragma unroll
+    for (int a = 0; a < kR; ++a) {
+      double s = 0.0;
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) {
+        const double df = ri[a][d] - cj[d];
+        s = (d == 0) ? df * df : fma(df, df, s);
+      }
+      const double e = exp_neg_table(s, table);
+      acc_r[a] = fma(e, xj, acc_r[a]);
+      acc_c[b] = fma(e, xi[a], acc_c[b]);
+    }
+  }
+  double* slot_row = S + ((long long)I * T + J) * kB;
+  double* slot_col = diag ? nullptr : S + ((long long)J * T + I) * kB;
+  store_sums<double>(acc_r, acc_c, slot_row, slot_col, colbuf, ty, tx);
+}
+
+// y_i = sum_K S[tile(i)][K][i % B] + nugget x_i
+__global__ void sym_f64_reduce_kernel(int n, int T, const double* __restrict__ S, const double* __restrict__ x,
+                                      double nugget, double* __restrict__ y, const int* __restrict__ skip) {
+  if (skip && *skip) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int tile = i / kB, r = i % kB;
+  const double* p = S + (long long)tile * T * kB + r;
+  double s = 0.0;
+#pragma unroll 4
+  for (int k = 0; k < T; ++k) s += __ldcg(p + (long long)k * kB);
+  y[i] = fma(nugget, x[i], s);
+}
+
+// ----------------------------------------------------------------- FP32
+template <int DIM>
+__global__ void __launch_bounds__(kThreads) sym_f32_pair_kernel(int n, int T, const float4* __restrict__ pts,
+                                                                const double* __restrict__ centers,
+                                                                const int* __restrict__ perm,
+                                                                const double* __restrict__ x, float* __restrict__ S,
+                                                                const int* __restrict__ skip) {
+  if (skip && *skip) return;
+  __shared__ float4 sp[2][kB];
+  __shared__ float colbuf[16 * kB];
+  int I, J;
+  pair_of(blockIdx.x, T, &I, &J);
+  for (int t = threadIdx.x; t < 2 * kB; t += kThreads) {
+    const int side = t / kB, k = t % kB;
+    const int g = (side ? J : I) * kB + k;
+    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (g < n) {
+      p = pts[g];
+      p.w = (float)x[perm[g]];
+    }
+    sp[side][k] = p;
+  }
+  // centre difference of the two tiles, rounded once to FP32
+  float dc[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) dc[d] = (float)(centers[3 * I + d] - centers[3 * J + d]);
+  __syncthreads();
+  const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
+  float ri[kR][DIM], xi[kR];
+#pragma unroll
+  for (int a = 0; a < kR; ++a) {
+    const float4 p = sp[0][ty + 16 * a];
+    ri[a][0] = p.x + dc[0];
+    if (DIM > 1) ri[a][1 % DIM] = p.y + dc[1];
+    if (DIM > 2) ri[a][2 % DIM] = p.z + dc[2];
+    xi[a] = p.w;
+  }
+  float acc_r[kR], acc_c[kC];
+#pragma unroll
+  for (int a = 0; a < kR; ++a) acc_r[a] = 0.f;
+#pragma unroll
+  for (int b = 0; b < kC; ++b) acc_c[b] = 0.f;
+  const bool diag = (I == J);
+#pragma unroll
+  for (int b = 0; b < kC; ++b) {
+    const float4 q = sp[1][tx + 16 * b];
+#pragma unroll
+    for (int a = 0; a < kR; ++a) {
+      const float dx = ri[a][0] - q.x;
+      float ns;
+      if (DIM == 1) {
+        ns = -dx * dx;
+      } else if (DIM == 2) {
+        const float dy = ri[a][1 % DIM] - q.y;
+        ns = fmaf(-dx, dx, -dy * dy);
+      } else {
+        const float dy = ri[a][1 % DIM] - q.y;
+        const float dz = ri[a][2 % DIM] - q.z;
+        ns = fmaf(-dx, dx, fmaf(-dy, dy, -dz * dz));
+      }
+      const float e = ex2_approx(ns);
+      acc_r[a] = fmaf(e, q.w, acc_r[a]);
+      acc_c[b] = fmaf(e, xi[a], acc_c[b]);
+    }
+  }
+  float* slot_row = S + ((long long)I * T + J) * kB;
+  float* slot_col = diag ? nullptr : S + ((long long)J * T + I) * kB;
+  store_sums<float>(acc_r, acc_c, slot_row, slot_col, colbuf, ty, tx);
+}
+
+__global__ void sym_f32_reduce_kernel(int n, int T, const float* __restrict__ S, const int* __restrict__ perm,
+                                      const double* __restrict__ x, double nugget, double* __restrict__ y,
+                                      const int* __restrict__ skip) {
+  if (skip && *skip) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int tile = i / kB, r = i % kB;
+  const float* p = S + (long long)tile * T * kB + r;
+  double s = 0.0;
+#pragma unroll 4
+  for (int k = 0; k < T; ++k) s += (double)__ldcg(p + (long long)k * kB);
+  const int o = perm[i];
+  y[o] = fma(nugget, x[o], s);
+}
+
+// Morton (Z-order) key of a point quantised to 21 bits per axis.
+uint64_t spread3(uint64_t v) {
+  v &= 0x1fffff;
+  v = (v | v << 32) & 0x1f00000000ffffULL;
+  v = (v | v << 16) & 0x1f0000ff0000ffULL;
+  v = (v | v << 8) & 0x100f00f00f00f00fULL;
+  v = (v | v << 4) & 0x10c30c30c30c30c3ULL;
+  v = (v | v << 2) & 0x1249249249249249ULL;
+  return v;
+}
+
+uint64_t spread2(uint64_t v) {
+  v &= 0xffffffffULL;
+  v = (v | v << 16) & 0x0000ffff0000ffffULL;
+  v = (v | v << 8) & 0x00ff00ff00ff00ffULL;
+  v = (v | v << 4) & 0x0f0f0f0f0f0f0f0fULL;
+  v = (v | v << 2) & 0x3333333333333333ULL;
+  v = (v | v << 1) & 0x5555555555555555ULL;
+  return v;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- host side
+int sym_tiles(int n) { return (n + kB - 1) / kB; }
+
+SymF64::~SymF64() {
+  if (c_) pool_free(c_, S_);
+}
+
+int SymF64::init(DeviceContext* c, const GaussSystem& g) {
+  if (g.rows != g.cols || g.row_offset || g.col_offset || g.dim < 1 || g.dim > 3 ||
+      g.nugget_rule != MGB_NUGGET_DIAGONAL)
+    return set_error(MGB_ERR_ARG, "symmetric FP64 matvec: square d<=3 systems with a diagonal nugget only");
+  c_ = c;
+  g_ = g;
+  T_ = sym_tiles(g.rows);
+  return pool_alloc(c, sizeof(double) * (size_t)T_ * T_ * kB, (void**)&S_);
+}
+
+int SymF64::apply(const double* x, double* y, cudaStream_t s, const int* skip) {
+  const long long pairs = (long long)T_ * (T_ + 1) / 2;
+  if (pairs > 0x7fffffffLL) return set_error(MGB_ERR_ARG, "system too large for one grid");
+  const double* c0 = g_.coords[0];
+  const double* c1 = g_.dim > 1 ? g_.coords[1] : c0;
+  const double* c2 = g_.dim > 2 ? g_.coords[2] : c0;
+  switch (g_.dim) {
+    case 1: sym_f64_pair_kernel<1><<<(unsigned)pairs, kThreads, 0, s>>>(g_.rows, T_, c0, c1, c2, x, c_->exp_table, S_, skip); break;
+    case 2: sym_f64_pair_kernel<2><<<(unsigned)pairs, kThreads, 0, s>>>(g_.rows, T_, c0, c1, c2, x, c_->exp_table, S_, skip); break;
+    default: sym_f64_pair_kernel<3><<<(unsigned)pairs, kThreads, 0, s>>>(g_.rows, T_, c0, c1, c2, x, c_->exp_table, S_, skip); break;
+  }
+  sym_f64_reduce_kernel<<<(g_.rows + 255) / 256, 256, 0, s>>>(g_.rows, T_, S_, x, g_.nugget, y, skip);
+  count_launches(2);
+  MGB_CUDA(cudaGetLastError());
+  return MGB_OK;
+}
+
+SymF32::~SymF32() {
+  if (c_) {
+    pool_free(c_, S_);
+    pool_free(c_, pts_);
+  }
+}
+
+int SymF32::init(DeviceContext* c, const GaussSystem& g, cudaStream_t s) {
+  if (g.rows != g.cols || g.row_offset || g.col_offset || g.dim < 1 || g.dim > 3 ||
+      g.nugget_rule != MGB_NUGGET_DIAGONAL)
+    return set_error(MGB_ERR_ARG, "mixed matvec: square d<=3 systems with a diagonal nugget only");
+  c_ = c;
+  n_ = g.rows;
+  dim_ = g.dim;
+  nugget_ = g.nugget;
+  T_ = sym_tiles(n_);
+  // coordinates to the host once per system: Morton order, tile centres
+  std::vector<double> h((size_t)n_ * dim_);
+  for (int d = 0; d < dim_; ++d)
+    MGB_CUDA(cudaMemcpyAsync(h.data() + (size_t)d * n_, g.coords[d], sizeof(double) * n_, cudaMemcpyDeviceToHost, s));
+  MGB_CUDA(cudaStreamSynchronize(s));
+  const double scale = std::sqrt(1.4426950408889634);  // sqrt(log2 e): exp(-s) = 2^(-s log2 e)
+  double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  for (int d = 0; d < dim_; ++d) {
+    lo[d] = hi[d] = h[(size_t)d * n_];
+    for (int i = 0; i < n_; ++i) {
+      lo[d] = std::min(lo[d], h[(size_t)d * n_ + i]);
+      hi[d] = std::max(hi[d], h[(size_t)d * n_ + i]);
+    }
+  }
+  std::vector<uint64_t> key(n_);
+  for (int i = 0; i < n_; ++i) {
+    uint64_t q[3] = {0, 0, 0};
+    for (int d = 0; d < dim_; ++d) {
+      const double span = hi[d] > lo[d] ? hi[d] - lo[d] : 1.0;
+      const double u = (h[(size_t)d * n_ + i] - lo[d]) / span;
+      const double bits = dim_ == 3 ? 2097151.0 : 4294967295.0;
+      q[d] = (uint64_t)std::min(bits, std::max(0.0, u * bits));
+    }
+    key[i] = dim_ == 3 ? (spread3(q[0]) | spread3(q[1]) << 1 | spread3(q[2]) << 2)
+                       : (dim_ == 2 ? (spread2(q[0]) | spread2(q[1]) << 1) : q[0]);
+  }
+  std::vector<int> perm(n_);
+  std::iota(perm.begin(), perm.end(), 0);
+  std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) { return key[a] < key[b]; });
+  std::vector<double> centers((size_t)3 * T_, 0.0);
+  std::vector<float4> pts((size_t)T_ * kB);
+  for (int t = 0; t < T_; ++t) {
+    const int b0 = t * kB, b1 = std::min(n_, b0 + kB);
+    for (int d = 0; d < dim_; ++d) {
+      double acc = 0.0;
+      for (int k = b0; k < b1; ++k) acc += h[(size_t)d * n_ + perm[k]] * scale;
+      centers[3 * t + d] = acc / (b1 - b0);
+    }
+    for (int k = b0; k < t * kB + kB; ++k) {
+      float v[3] = {0.f, 0.f, 0.f};
+      if (k < b1)
+        for (int d = 0; d < dim_; ++d) v[d] = (float)(h[(size_t)d * n_ + perm[k]] * scale - centers[3 * t + d]);
+      pts[k] = make_float4(v[0], v[1], v[2], 0.f);
+    }
+  }
+  const size_t bytes_pts = sizeof(float4) * pts.size();
+  const size_t bytes_ctr = sizeof(double) * centers.size();
+  const size_t bytes_perm = sizeof(int) * (size_t)n_;
+  MGB_TRY(pool_alloc(c, bytes_pts + bytes_ctr + bytes_perm, (void**)&pts_));
+  centers_ = reinterpret_cast<double*>(reinterpret_cast<char*>(pts_) + bytes_pts);
+  perm_ = reinterpret_cast<int*>(reinterpret_cast<char*>(centers_) + bytes_ctr);
+  MGB_CUDA(cudaMemcpyAsync(pts_, pts.data(), bytes_pts, cudaMemcpyHostToDevice, s));
+  MGB_CUDA(cudaMemcpyAsync(centers_, centers.data(), bytes_ctr, cudaMemcpyHostToDevice, s));
+  MGB_CUDA(cudaMemcpyAsync(perm_, perm.data(), bytes_perm, cudaMemcpyHostToDevice, s));
+  MGB_TRY(pool_alloc(c, sizeof(float) * (size_t)T_ * T_ * kB, (void**)&S_));
+  MGB_CUDA(cudaStreamSynchronize(s));
+  return MGB_OK;
+}
+
+int SymF32::apply(const double* x, double* y, cudaStream_t s, const int* skip) {
+  const long long pairs = (long long)T_ * (T_ + 1) / 2;
+  if (pairs > 0x7fffffffLL) return set_error(MGB_ERR_ARG, "system too large for one grid");
+  switch (dim_) {
+    case 1: sym_f32_pair_kernel<1><<<(unsigned)pairs, kThreads, 0, s>>>(n_, T_, pts_, centers_, perm_, x, S_, skip); break;
+    case 2: sym_f32_pair_kernel<2><<<(unsigned)pairs, kThreads, 0, s>>>(n_, T_, pts_, centers_, perm_, x, S_, skip); break;
+    default: sym_f32_pair_kernel<3><<<(unsigned)pairs, kThreads, 0, s>>>(n_, T_, pts_, centers_, perm_, x, S_, skip); break;
+  }
+  sym_f32_reduce_kernel<<<(n_ + 255) / 256, 256, 0, s>>>(n_, T_, S_, perm_, x, nugget_, y, skip);
+  count_launches(2);
+  MGB_CUDA(cudaGetLastError());
+  return MGB_OK;
+}
+
+}  // namespace mgb

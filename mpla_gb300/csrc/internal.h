@@ -125,13 +125,6 @@ int launch_gauss_f64(DeviceContext* c, const GaussSystem& g, const double* x, do
 int launch_gauss_entries_f64(DeviceContext* c, const GaussSystem& g, int count, const int* i,
                              const int* j, double* out, cudaStream_t s);
 
-// Mixed-precision square Gaussian matvec; workspace prepared once per system.
-struct MixedSystem;
-int mixed_prepare(DeviceContext* c, const GaussSystem& g, MixedSystem** out, cudaStream_t s);
-int launch_gauss_mixed(DeviceContext* c, MixedSystem* m, const double* x, double* y,
-                       cudaStream_t s, const int* done);
-void mixed_release(DeviceContext* c, MixedSystem* m);
-
 // BLAS-1 and fused Krylov vector kernels (blas1.cu).
 int launch_dot(DeviceContext* c, int n, const double* x, const double* y, double* out_dev,
                cudaStream_t s);

@@ -32,7 +32,9 @@ class DenseMatvec : public Matvec {
   int lda_;
 };
 
-// Gaussian kernel matrix, FP64 fused matvec (coordinates scaled once).
+// Gaussian kernel matrix, FP64 fused matvec: the symmetric tile-pair kernel
+// for square systems with d <= 3 and the diagonal nugget, the rectangular
+// kernel otherwise (kernel.cu nugget rule, d > 3).
 class GaussF64Matvec : public Matvec {
  public:
   ~GaussF64Matvec() override;
@@ -44,10 +46,10 @@ class GaussF64Matvec : public Matvec {
   DeviceContext* c_ = nullptr;
   GaussSystem g_{};
   ScaledCoords sc_;
+  Matvec* sym_ = nullptr;
 };
 
-// Gaussian kernel matrix, FP32/SFU matvec (square systems).
-struct MixedSystem;
+// Gaussian kernel matrix, FP32/SFU symmetric matvec (square systems).
 class GaussMixedMatvec : public Matvec {
  public:
   ~GaussMixedMatvec() override;
@@ -56,8 +58,7 @@ class GaussMixedMatvec : public Matvec {
   int n() const override { return n_; }
 
  private:
-  DeviceContext* c_ = nullptr;
-  MixedSystem* m_ = nullptr;
+  Matvec* impl_ = nullptr;
   int n_ = 0;
 };
 

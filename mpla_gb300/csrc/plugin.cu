@@ -54,6 +54,22 @@ __global__ void k_create_gauss(gaussian_kernel_system_assembler** out, double** 
   *out = a;
 }
 
+// The object lives on the device heap (in-kernel new), which runtime copies
+// cannot address, so its fields are read by a kernel into pool memory.
+struct GaussFields {
+  double** points;
+  double regularization;
+  int dim;
+  int max_rows;
+};
+
+__global__ void k_read_gauss(const gaussian_kernel_system_assembler* obj, GaussFields* out) {
+  out->points = obj->points;
+  out->regularization = obj->regularization;
+  out->dim = obj->dim;
+  out->max_rows = obj->max_row_count_per_dgemv;
+}
+
 __global__ void k_destroy_gauss(gaussian_kernel_system_assembler** obj) {
   delete *obj;
   *obj = nullptr;
@@ -172,19 +188,28 @@ int assembler_system(const void* obj, const mpla_generic_matrix* A, GaussSystem*
   }
   // Field values are read from the device object on every call, so a caller
   // that patches points or regularization in place is honoured.
-  alignas(16) unsigned char raw[sizeof(gaussian_kernel_system_assembler)];
-  MGB_CUDA(cudaMemcpy(raw, obj, sizeof(raw), cudaMemcpyDeviceToHost));
-  const gaussian_kernel_system_assembler* h = reinterpret_cast<const gaussian_kernel_system_assembler*>(raw);
-  if (h->dim < 1 || h->dim > kMaxGaussDim)
-    return set_error(MGB_ERR_ARG, "assembler dim %d not in [1,%d]", h->dim, kMaxGaussDim);
+  DeviceContext* c = nullptr;
+  MGB_TRY(context(&c));
+  GaussFields* dev = nullptr;
+  MGB_TRY(pool_alloc(c, sizeof(GaussFields), (void**)&dev));
+  k_read_gauss<<<1, 1, 0, c->stream>>>(static_cast<const gaussian_kernel_system_assembler*>(obj), dev);
+  count_launches(1);
+  GaussFields h;
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, dev, sizeof(h), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  pool_free(c, dev);
+  if (e != cudaSuccess) return cuda_error(e, "reading the assembler object", __FILE__, __LINE__);
+  if (h.dim < 1 || h.dim > kMaxGaussDim)
+    return set_error(MGB_ERR_ARG, "assembler dim %d not in [1,%d]", h.dim, kMaxGaussDim);
   memset(g, 0, sizeof(*g));
-  g->dim = h->dim;
-  MGB_CUDA(cudaMemcpy(g->coords, h->points, sizeof(double*) * h->dim, cudaMemcpyDeviceToHost));
+  g->dim = h.dim;
+  MGB_CUDA(cudaMemcpy(g->coords, h.points, sizeof(double*) * h.dim, cudaMemcpyDeviceToHost));
   g->rows = A->cur_proc_row_count;
   g->cols = A->cur_proc_col_count;
   g->row_offset = A->cur_proc_row_offset;
   g->col_offset = A->cur_proc_col_offset;
-  g->nugget = h->regularization;
+  g->nugget = h.regularization;
   g->nugget_rule = MGB_NUGGET_DIAGONAL;
   return MGB_OK;
 }

@@ -1,0 +1,63 @@
+"""Small, self-contained kernel workloads for Nsight Compute captures.
+
+Each case launches one hot kernel a few times on inputs sized for a capture
+that ends by itself (a few hundred MB on the device at most):
+
+  python -m mpla_gb300.profile_cases dgemv       # dense dgemv, n = 4096 (134 MB matrix)
+  python -m mpla_gb300.profile_cases gauss_f64   # FP64 Gaussian matvec, n = 16384, d = 2
+  python -m mpla_gb300.profile_cases gauss_mixed # FP32/SFU Gaussian matvec, n = 65536, d = 2
+  python -m mpla_gb300.profile_cases all
+
+Prints the CUDA-event time per launch of each case.
+"""
+from __future__ import annotations
+
+import sys
+
+import numpy as np
+
+import mpla_gb300 as mg
+from mpla_gb300 import synth
+
+
+def case_dgemv(reps=3):
+    n = 4096
+    rng = np.random.default_rng(0)
+    A = mg.DeviceArray.from_numpy(rng.uniform(-1, 1, n * n))
+    x = mg.DeviceArray.from_numpy(rng.uniform(-1, 1, n))
+    y = mg.DeviceArray(n)
+    ms = mg.time_dgemv(n, A.ptr, x.ptr, y.ptr, reps=reps)
+    print(f"dgemv n={n}: {ms:.4f} ms/launch, {(8.0 * n * n + 16 * n) / ms / 1e6:.1f} GB/s")
+
+
+def _gauss(n, dim, ell, precision, reps):
+    prob = synth.gauss_problem(n, dim, ell, 1e-4, seed=0)
+    dp = mg.GaussPoints(prob.scaled())
+    x = mg.DeviceArray.from_numpy(np.random.default_rng(1).standard_normal(n))
+    y = mg.DeviceArray(n)
+    ms = mg.time_gauss_matvec(dp, 1e-4, precision, x.ptr, y.ptr, reps=reps)
+    name = "fp64" if precision == mg.PREC_FP64 else "mixed"
+    print(f"gauss_{name} n={n} d={dim}: {ms:.4f} ms/launch, {float(n) * n / ms / 1e9:.2f} Gentries/s")
+
+
+def case_gauss_f64(reps=2):
+    _gauss(16384, 2, 0.05, mg.PREC_FP64, reps)
+
+
+def case_gauss_mixed(reps=3):
+    _gauss(65536, 2, 0.05, mg.PREC_MIXED, reps)
+
+
+CASES = {"dgemv": case_dgemv, "gauss_f64": case_gauss_f64, "gauss_mixed": case_gauss_mixed}
+
+
+def main(argv):
+    mg.init(0)
+    names = list(CASES) if (not argv or argv[0] == "all") else argv
+    for name in names:
+        CASES[name]()
+    mg.synchronize()
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])

@@ -41,7 +41,8 @@ def test_fp64_entries_within_ulps(gpu, orc, dim):
     want = np.array([op.entry(a, b) for a, b in zip(i, j)])
     nz = want > 1e-300
     rel = np.abs(got[nz] - want[nz]) / want[nz]
-    assert rel.max() <= 4 * 2.2e-16 * np.maximum(1.0, -np.log(want[nz]))
+    # exp(-s) is conditioned like s: allow 4 ulp x max(1, s)
+    assert np.all(rel <= 4 * 2.2e-16 * np.maximum(1.0, -np.log(want[nz])))
 
 
 @pytest.mark.parametrize("n,dim,ell", [(1, 2, 0.1), (37, 2, 0.1), (1000, 1, 0.05), (2048, 2, 0.05),
