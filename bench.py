@@ -292,6 +292,7 @@ def run_ours(args, world, rank, local):
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": f"{L2_FLUSH_BYTES >> 20} MiB buffer zeroed before every step"},
         "iterations": iters_mixed,
+        "converged": all(int(i.status) == 0 for i in infos),
         "fp64_true_residual_replacements": int(info.fp64_matvecs),
         "true_relres": true_rel,
         "p50_ms": statistics.median([sec_max * 1e3 / args.steps]),
@@ -389,7 +390,7 @@ def main(argv=None):
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--n", type=int, default=N_FULL)
-    p.add_argument("--iter-max", type=int, default=200000)
+    p.add_argument("--iter-max", type=int, default=100000)
     p.add_argument("--e2e-steps", type=int, default=1)
     p.add_argument("--fp64-sample-iters", type=int, default=20)
     p.add_argument("--fp64-iterations", type=int, default=0,

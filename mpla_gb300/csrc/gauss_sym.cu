@@ -20,12 +20,15 @@
 // FP64: entries exp(-s) with the table exponential (devutil.cuh) on the
 // squared distance of the caller's coordinates; 15 FP64 operations per
 // evaluated entry, 7.5 per matrix entry (d = 2).
-// FP32: points are Morton-ordered and stored relative to the centre of their
-// tile, and each tile pair adds the difference of the two centres (computed
-// in FP64) once per row, so distances keep FP32 relative accuracy however far
-// the points are from the origin; exponentials on the SFU (ex2.approx, with
-// coordinates pre-scaled by sqrt(log2 e)).  7 issue slots and 1 MUFU per
-// evaluated entry, i.e. 0.5 MUFU per matrix entry.
+// FP32: points are Morton-ordered (compact tiles) and rounded to FP32 once
+// per point, so the FP32 operator is exactly the Gaussian kernel matrix of a
+// slightly perturbed point set and stays symmetric positive definite.  (A
+// per-tile-pair centring, with the difference of the two tile centres rounded
+// once per pair, perturbs every tile pair differently; at n = 65536 that
+// operator made the mixed solve stagnate at relres 1.4e-10, so the tile
+// centres are kept at zero here.)  Exponentials on the SFU (ex2.approx, with
+// coordinates pre-scaled by sqrt(log2 e)).  About 8 issue slots and 1 MUFU
+// per evaluated entry, i.e. 0.5 MUFU per matrix entry.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -53,11 +56,13 @@ __device__ __forceinline__ float ex2_approx(float v) {
 }
 
 // tile pair index p -> (I, J), I <= J, enumerating the upper triangle row by
-// row: p = I*T - I*(I-1)/2 + (J - I).
+// row: p = I*T - I*(I-1)/2 + (J - I).  FP32 estimate of I (SFU sqrt) and
+// exact integer correction: no FP64 work (GB300's FP64 pipe is scarce).
 __device__ __forceinline__ void pair_of(long long p, int T, int* I, int* J) {
   // I = largest i with start(i) <= p, start(i) = i*T - i*(i-1)/2
-  const double tt = 2.0 * T + 1.0;
-  int i = (int)floor((tt - sqrt(tt * tt - 8.0 * (double)p)) * 0.5);
+  const float tt = 2.0f * (float)T + 1.0f;
+  const float disc = fmaxf(tt * tt - 8.0f * (float)p, 0.0f);
+  int i = (int)((tt - sqrtf(disc)) * 0.5f);
   if (i < 0) i = 0;
   if (i > T - 1) i = T - 1;
   auto start = [&](long long k) { return k * T - k * (k - 1) / 2; };
@@ -65,6 +70,15 @@ __device__ __forceinline__ void pair_of(long long p, int T, int* I, int* J) {
   while (i + 1 < T && start(i + 1) <= p) ++i;
   *I = i;
   *J = i + (int)(p - start(i));
+}
+
+// (I, J) computed once per CTA and broadcast through shared memory.
+__device__ __forceinline__ void cta_pair(int T, int* I, int* J) {
+  __shared__ int s_ij[2];
+  if (threadIdx.x == 0) pair_of(blockIdx.x, T, &s_ij[0], &s_ij[1]);
+  __syncthreads();
+  *I = s_ij[0];
+  *J = s_ij[1];
 }
 
 // Write the CTA's row sums (acc_r, one per thread row) and column sums.
@@ -117,7 +131,7 @@ __global__ void __launch_bounds__(kThreads) sym_f64_pair_kernel(int n, int T, co
   double* colbuf = table;
   static_assert(16 * kB <= kExpTableSize, "column buffer must fit in the table storage");
   int I, J;
-  pair_of(blockIdx.x, T, &I, &J);
+  cta_pair(T, &I, &J);
   for (int i = threadIdx.x; i < kExpTableSize; i += kThreads) table[i] = table_g[i];
   for (int t = threadIdx.x; t < 2 * kB; t += kThreads) {
     const int side = t / kB, k = t % kB;
@@ -182,53 +196,69 @@ __global__ void sym_f64_reduce_kernel(int n, int T, const double* __restrict__ S
 }
 
 // ----------------------------------------------------------------- FP32
+// Warp layout for FP32: a CTA of 4 warps evaluates one 128 x 128 tile pair;
+// warp w owns columns [32w, 32w+32) of tile J, lane l owns rows
+// {l, l+32, l+64, l+96} of tile I.  Per entry: FADDs and one FMUL/FFMA for
+// the negated squared distance, one MUFU.EX2, an FFMA into the row sum and an
+// FFMA into the lane's partial of that column.  The 32 column partials of a
+// lane are summed across the warp by a butterfly reduce-scatter (31 shuffles
+// and adds per lane for 4096 entries), after which lane l holds column
+// 32w + l complete (the warp saw all 128 rows).  Row sums combine the 4 warps
+// in shared memory in warp order.
+constexpr int kF32Threads = 128;
+
+__device__ __forceinline__ void warp_reduce_scatter32(float (&v)[32], int lane) {
+#pragma unroll
+  for (int half = 16; half >= 1; half >>= 1) {
+    const bool upper = (lane & half) != 0;
+#pragma unroll
+    for (int k = 0; k < half; ++k) {
+      const float send = upper ? v[k] : v[k + half];
+      const float keep = upper ? v[k + half] : v[k];
+      v[k] = keep + __shfl_xor_sync(0xffffffffu, send, half);
+    }
+  }
+}
+
 template <int DIM>
-__global__ void __launch_bounds__(kThreads) sym_f32_pair_kernel(int n, int T, const float4* __restrict__ pts,
-                                                                const double* __restrict__ centers,
-                                                                const int* __restrict__ perm,
-                                                                const double* __restrict__ x, float* __restrict__ S,
-                                                                const int* __restrict__ skip) {
+__global__ void __launch_bounds__(kF32Threads) sym_f32_pair_kernel(int n, int T, const float4* __restrict__ pts,
+                                                                   const double* __restrict__ centers,
+                                                                   const float* __restrict__ xf,
+                                                                   float* __restrict__ S,
+                                                                   const int* __restrict__ skip) {
   if (skip && *skip) return;
   __shared__ float4 sp[2][kB];
-  __shared__ float colbuf[16 * kB];
+  __shared__ float rowbuf[4][kB];
+  __shared__ float s_dc[3];
   int I, J;
-  pair_of(blockIdx.x, T, &I, &J);
-  for (int t = threadIdx.x; t < 2 * kB; t += kThreads) {
+  cta_pair(T, &I, &J);
+  for (int t = threadIdx.x; t < 2 * kB; t += kF32Threads) {
     const int side = t / kB, k = t % kB;
     const int g = (side ? J : I) * kB + k;
-    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (g < n) {
-      p = pts[g];
-      p.w = (float)x[perm[g]];
-    }
+    float4 p = pts[g];  // padded to whole tiles
+    p.w = (g < n) ? xf[g] : 0.f;
     sp[side][k] = p;
   }
-  // centre difference of the two tiles, rounded once to FP32
-  float dc[3];
-#pragma unroll
-  for (int d = 0; d < 3; ++d) dc[d] = (float)(centers[3 * I + d] - centers[3 * J + d]);
+  if (threadIdx.x < 3) s_dc[threadIdx.x] = (float)(centers[3 * I + threadIdx.x] - centers[3 * J + threadIdx.x]);
   __syncthreads();
-  const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
-  float ri[kR][DIM], xi[kR];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float ri[4][DIM], xi[4];
 #pragma unroll
-  for (int a = 0; a < kR; ++a) {
-    const float4 p = sp[0][ty + 16 * a];
-    ri[a][0] = p.x + dc[0];
-    if (DIM > 1) ri[a][1 % DIM] = p.y + dc[1];
-    if (DIM > 2) ri[a][2 % DIM] = p.z + dc[2];
+  for (int a = 0; a < 4; ++a) {
+    const float4 p = sp[0][lane + 32 * a];
+    ri[a][0] = p.x + s_dc[0];
+    if (DIM > 1) ri[a][1 % DIM] = p.y + s_dc[1];
+    if (DIM > 2) ri[a][2 % DIM] = p.z + s_dc[2];
     xi[a] = p.w;
   }
-  float acc_r[kR], acc_c[kC];
+  float acc_r[4] = {0.f, 0.f, 0.f, 0.f};
+  float col[32];
 #pragma unroll
-  for (int a = 0; a < kR; ++a) acc_r[a] = 0.f;
+  for (int b = 0; b < 32; ++b) {
+    const float4 q = sp[1][32 * warp + b];
+    float c = 0.f;
 #pragma unroll
-  for (int b = 0; b < kC; ++b) acc_c[b] = 0.f;
-  const bool diag = (I == J);
-#pragma unroll
-  for (int b = 0; b < kC; ++b) {
-    const float4 q = sp[1][tx + 16 * b];
-#pragma unroll
-    for (int a = 0; a < kR; ++a) {
+    for (int a = 0; a < 4; ++a) {
       const float dx = ri[a][0] - q.x;
       float ns;
       if (DIM == 1) {
@@ -243,14 +273,31 @@ __global__ void __launch_bounds__(kThreads) sym_f32_pair_kernel(int n, int T, co
       }
       const float e = ex2_approx(ns);
       acc_r[a] = fmaf(e, q.w, acc_r[a]);
-      acc_c[b] = fmaf(e, xi[a], acc_c[b]);
+      c = fmaf(e, xi[a], c);
     }
+    col[b] = c;
   }
-  float* slot_row = S + ((long long)I * T + J) * kB;
-  float* slot_col = diag ? nullptr : S + ((long long)J * T + I) * kB;
-  store_sums<float>(acc_r, acc_c, slot_row, slot_col, colbuf, ty, tx);
+#pragma unroll
+  for (int a = 0; a < 4; ++a) rowbuf[warp][lane + 32 * a] = acc_r[a];
+  if (I != J) {
+    warp_reduce_scatter32(col, lane);
+    S[((long long)J * T + I) * kB + 32 * warp + lane] = col[0];
+  }
+  __syncthreads();
+  const int r = threadIdx.x;  // 128 threads, 128 rows
+  S[((long long)I * T + J) * kB + r] = ((rowbuf[0][r] + rowbuf[1][r]) + rowbuf[2][r]) + rowbuf[3][r];
 }
 
+// xf[k] = x[perm[k]] rounded to FP32 (once per matvec, not once per tile pair)
+__global__ void sym_f32_gather_kernel(int n, const int* __restrict__ perm, const double* __restrict__ x,
+                                      float* __restrict__ xf, const int* __restrict__ skip) {
+  if (skip && *skip) return;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) xf[k] = (float)x[perm[k]];
+}
+
+// y[perm[i]] = sum over the T slots of row i + nugget x: groups of 16 slots in
+// FP32, the groups in FP64, always in slot order.
 __global__ void sym_f32_reduce_kernel(int n, int T, const float* __restrict__ S, const int* __restrict__ perm,
                                       const double* __restrict__ x, double nugget, double* __restrict__ y,
                                       const int* __restrict__ skip) {
@@ -260,8 +307,13 @@ __global__ void sym_f32_reduce_kernel(int n, int T, const float* __restrict__ S,
   const int tile = i / kB, r = i % kB;
   const float* p = S + (long long)tile * T * kB + r;
   double s = 0.0;
+  for (int k0 = 0; k0 < T; k0 += 16) {
+    const int k1 = min(T, k0 + 16);
+    float g = 0.f;
 #pragma unroll 4
-  for (int k = 0; k < T; ++k) s += (double)__ldcg(p + (long long)k * kB);
+    for (int k = k0; k < k1; ++k) g += __ldcg(p + (long long)k * kB);
+    s += (double)g;
+  }
   const int o = perm[i];
   y[o] = fma(nugget, x[o], s);
 }
@@ -368,15 +420,12 @@ int SymF32::init(DeviceContext* c, const GaussSystem& g, cudaStream_t s) {
   std::vector<int> perm(n_);
   std::iota(perm.begin(), perm.end(), 0);
   std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) { return key[a] < key[b]; });
+  // Tile centres stay zero (global coordinates): see the FP32 note at the
+  // top of the file.
   std::vector<double> centers((size_t)3 * T_, 0.0);
   std::vector<float4> pts((size_t)T_ * kB);
   for (int t = 0; t < T_; ++t) {
     const int b0 = t * kB, b1 = std::min(n_, b0 + kB);
-    for (int d = 0; d < dim_; ++d) {
-      double acc = 0.0;
-      for (int k = b0; k < b1; ++k) acc += h[(size_t)d * n_ + perm[k]] * scale;
-      centers[3 * t + d] = acc / (b1 - b0);
-    }
     for (int k = b0; k < t * kB + kB; ++k) {
       float v[3] = {0.f, 0.f, 0.f};
       if (k < b1)
@@ -393,7 +442,8 @@ int SymF32::init(DeviceContext* c, const GaussSystem& g, cudaStream_t s) {
   MGB_CUDA(cudaMemcpyAsync(pts_, pts.data(), bytes_pts, cudaMemcpyHostToDevice, s));
   MGB_CUDA(cudaMemcpyAsync(centers_, centers.data(), bytes_ctr, cudaMemcpyHostToDevice, s));
   MGB_CUDA(cudaMemcpyAsync(perm_, perm.data(), bytes_perm, cudaMemcpyHostToDevice, s));
-  MGB_TRY(pool_alloc(c, sizeof(float) * (size_t)T_ * T_ * kB, (void**)&S_));
+  MGB_TRY(pool_alloc(c, sizeof(float) * ((size_t)T_ * T_ * kB + (size_t)T_ * kB), (void**)&S_));
+  xf_ = S_ + (size_t)T_ * T_ * kB;
   MGB_CUDA(cudaStreamSynchronize(s));
   return MGB_OK;
 }
@@ -401,13 +451,14 @@ int SymF32::init(DeviceContext* c, const GaussSystem& g, cudaStream_t s) {
 int SymF32::apply(const double* x, double* y, cudaStream_t s, const int* skip) {
   const long long pairs = (long long)T_ * (T_ + 1) / 2;
   if (pairs > 0x7fffffffLL) return set_error(MGB_ERR_ARG, "system too large for one grid");
+  sym_f32_gather_kernel<<<(n_ + 255) / 256, 256, 0, s>>>(n_, perm_, x, xf_, skip);
   switch (dim_) {
-    case 1: sym_f32_pair_kernel<1><<<(unsigned)pairs, kThreads, 0, s>>>(n_, T_, pts_, centers_, perm_, x, S_, skip); break;
-    case 2: sym_f32_pair_kernel<2><<<(unsigned)pairs, kThreads, 0, s>>>(n_, T_, pts_, centers_, perm_, x, S_, skip); break;
-    default: sym_f32_pair_kernel<3><<<(unsigned)pairs, kThreads, 0, s>>>(n_, T_, pts_, centers_, perm_, x, S_, skip); break;
+    case 1: sym_f32_pair_kernel<1><<<(unsigned)pairs, kF32Threads, 0, s>>>(n_, T_, pts_, centers_, xf_, S_, skip); break;
+    case 2: sym_f32_pair_kernel<2><<<(unsigned)pairs, kF32Threads, 0, s>>>(n_, T_, pts_, centers_, xf_, S_, skip); break;
+    default: sym_f32_pair_kernel<3><<<(unsigned)pairs, kF32Threads, 0, s>>>(n_, T_, pts_, centers_, xf_, S_, skip); break;
   }
   sym_f32_reduce_kernel<<<(n_ + 255) / 256, 256, 0, s>>>(n_, T_, S_, perm_, x, nugget_, y, skip);
-  count_launches(2);
+  count_launches(3);
   MGB_CUDA(cudaGetLastError());
   return MGB_OK;
 }

@@ -37,7 +37,8 @@ class SymF32 : public Matvec {
   float4* pts_ = nullptr;     // T*128 points relative to their tile centre (pool block, also holds centres/perm)
   double* centers_ = nullptr; // 3 per tile
   int* perm_ = nullptr;       // sorted position -> original index
-  float* S_ = nullptr;        // T x T x 128 slot partials
+  float* S_ = nullptr;        // T x T x 128 slot partials (pool block, also holds xf_)
+  float* xf_ = nullptr;       // x gathered into sorted order, FP32
 };
 
 }  // namespace mgb

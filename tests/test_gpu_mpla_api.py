@@ -103,10 +103,13 @@ def test_assembler_plugin_cg_and_bicgstab_match_oracle(driver, orc, tmp_path, wh
         _, ko, _, _, hist = orc.bicgstab(op, b, iter_max=5000, eps=1e-10, history=True)
     else:
         _, ko, _, _, hist = orc.cg(op, b, iter_max=20000, eps=1e-10, history=True)
-    early = [k for k in sorted(printed) if k <= 12]
+    # six printed digits; BiCGSTAB amplifies last-bit differences of the
+    # matvec within a few iterations, CG much later
+    last, tol = (6, 5e-6) if which == 2 else (12, 2e-6)
+    early = [k for k in sorted(printed) if k <= last]
     assert early, out[:500]
     for k in early:
-        assert printed[k] == pytest.approx(hist[k], rel=1e-6), k
+        assert printed[k] == pytest.approx(hist[k], rel=tol), k
 
 
 def test_kernel_descriptor_core_matches_oracle(driver, orc, tmp_path):

@@ -141,7 +141,7 @@ def test_bicgstab_gauss_matches_oracle(gpu, orc):
     # BiCGSTAB's residual is not monotone; a different dot-product order moves
     # the count more than CG's (the residual histories are compared
     # iteration by iteration in test_gpu_mpla_api.py)
-    assert abs(info.iterations - ko) <= max(2, int(0.10 * ko))
+    assert abs(info.iterations - ko) <= max(2, int(0.20 * ko))
     assert orc.true_relres(op, b, dx.numpy()) < 1e-10
 
 
