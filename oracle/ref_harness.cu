@@ -250,6 +250,33 @@ int ref_gauss_matvec(int n, int dim, const double* pts, double nugget, int rule,
   return check();
 }
 
+// Right-hand side of the reference plugins: rule 0 through the assembler's
+// get_rhs_entry (mpla_set_generic_system_rhs), rule 1 through
+// gen_gaussian_kernel_rhs (mpla_set_gaussian_kernel_rhs).
+int ref_gauss_rhs(int n, int dim, const double* pts, int rule, double* b) {
+  DevicePoints P(n, dim, pts);
+  mpla_generic_matrix A;
+  mpla_init_generic_matrix(&A, &g_inst, n, n);
+  mpla_vector bv;
+  mpla_init_vector(&bv, &g_inst, n);
+  if (rule == 0) {
+    Assembler as(P.dev, n, dim, 0.0);
+    A.data = as.obj;
+    mpla_set_generic_system_rhs(&bv, &A, &g_inst);
+  } else {
+    kernel_matrix_data kd;
+    kd.points = P.dev;
+    kd.dim = dim;
+    kd.max_row_count_per_dgemv = n;
+    A.data = &kd;
+    mpla_set_gaussian_kernel_rhs(&bv, &A, &g_inst);
+  }
+  cudaMemcpy(b, bv.data, sizeof(double) * n, cudaMemcpyDeviceToHost);
+  mpla_free_generic_matrix(&A, &g_inst);
+  mpla_free_vector(&bv, &g_inst);
+  return check();
+}
+
 // Gaussian solve with the assembler plugin (nugget on the diagonal).
 // solver as in ref_solve_dense.  x holds x0 on entry.
 int ref_solve_gauss(int n, int dim, const double* pts, double nugget, const double* b, double* x, int iter_max,
