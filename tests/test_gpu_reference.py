@@ -3,8 +3,8 @@
 The reference is compiled from its own sources (oracle/build_ref.py) and
 called through its public API (oracle/ref_harness.cu).  Same seeded inputs
 on both sides: dgemv to 1e-13 relative (the benchmark spec), kernel matvecs to 1e-13,
-dense CG iteration counts +-1, the Gaussian CG family within the documented
-+-3 %, BiCGSTAB within 20 %.
+dense CG iteration counts +-1, the Gaussian CG family within 1 % (nugget
+1e-2) and 3 % (nugget 1e-4), BiCGSTAB within 20 %.
 """
 import numpy as np
 import pytest
@@ -60,7 +60,9 @@ def test_dense_cg_iterations_match_reference(gpu):
     assert np.allclose(dx.numpy(), x_ref, rtol=1e-8, atol=1e-10)
 
 
-@pytest.mark.parametrize("nugget,band", [(1e-2, 1), (1e-4, 0.03)])
+# condition numbers near 1e3 (nugget 1e-2) and 1e7 (nugget 1e-4): a different
+# dot-product order moves FP64 CG by under 1 % and by a few % respectively
+@pytest.mark.parametrize("nugget,band", [(1e-2, 0.01), (1e-4, 0.03)])
 def test_gauss_cg_iterations_match_reference(gpu, nugget, band):
     n = 1024
     pts = synth.gauss_points(n, 2, 50) / (np.sqrt(2) * 0.05)
