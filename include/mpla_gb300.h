@@ -72,6 +72,24 @@ int mgb_host_free(void* ptr_host);
 /* y = A x, A m x n column-major.  Replaces the cublasDgemv of mpla_dgemv
  * (mpla.cpp:716-751) at the 1x1 process grid. */
 int mgb_dgemv(int m, int n, const double* A_dev, int lda, const double* x_dev, double* y_dev, void* stream);
+/* y = A x like mgb_dgemv, for callers that cannot allocate device memory.
+ * No counterpart in the reference.  Callers such as code running inside a
+ * CUDA stream capture, plugins whose host framework owns every device
+ * allocation, or latency-critical paths that must not take the allocator's
+ * implicit synchronisation cannot call cudaMalloc; this entry point calls no
+ * cudaMalloc, cudaFree or allocating library routine and never creates the
+ * library context.  Its scratch (split-K partials and arrival counters) is a
+ * fixed 8.1 MiB device array that every GPU loading the library holds until
+ * the process exits.  Limits: m <= 1,048,512 rows (16383 strips of 64; half
+ * that when lda is odd or A is not 16-byte aligned) and
+ * m * ceil(n / 4096) <= 1,048,576; larger sizes return MGB_ERR_ARG.
+ * All calls share that array: calls that overlap on the GPU (different
+ * streams, or several host threads) race and must be serialised by the
+ * caller.  The first call on a device resolves the array's device address
+ * (cudaGetSymbolAddress with that device current), so make that first call
+ * before any stream capture.  NULL `stream` is the legacy default stream. */
+int mgb_dgemv_noalloc(int m, int n, const double* A_dev, int lda, const double* x_dev, double* y_dev,
+                      void* stream);
 /* *result_host = <x, y>.  Replaces mpla_ddot (mpla.cpp:753-770). */
 int mgb_ddot(int n, const double* x_dev, const double* y_dev, double* result_host, void* stream);
 /* y += alpha x.  Replaces mpla_daxpy (mpla.cpp:806-810). */

@@ -38,7 +38,7 @@ C_ABI_SYMBOLS = (
     "mgb_version", "mgb_last_error", "mgb_init", "mgb_shutdown", "mgb_device_sync",
     "mgb_malloc", "mgb_free", "mgb_memcpy_htod", "mgb_memcpy_dtoh", "mgb_memset",
     "mgb_host_alloc", "mgb_host_free",
-    "mgb_dgemv", "mgb_ddot", "mgb_daxpy",
+    "mgb_dgemv", "mgb_dgemv_noalloc", "mgb_ddot", "mgb_daxpy",
     "mgb_gauss_matvec_f64", "mgb_gauss_matvec_mixed", "mgb_gauss_entries_f64",
     "mgb_cg_dense", "mgb_bicgstab_dense", "mgb_cg_gauss", "mgb_bicgstab_gauss", "mgb_cg_gauss_host",
     "mgb_kernel_launches", "mgb_time_gauss_matvec", "mgb_time_dgemv",
@@ -87,6 +87,7 @@ _SIGS = {
     "mgb_host_alloc": (_I, [C.POINTER(_P), C.c_size_t]),
     "mgb_host_free": (_I, [_P]),
     "mgb_dgemv": (_I, [_I, _I, _P, _I, _P, _P, _P]),
+    "mgb_dgemv_noalloc": (_I, [_I, _I, _P, _I, _P, _P, _P]),
     "mgb_ddot": (_I, [_I, _P, _P, C.POINTER(_D), _P]),
     "mgb_daxpy": (_I, [_I, _D, _P, _P, _P]),
     "mgb_gauss_matvec_f64": (_I, [_I, _I, _I, _I, _I, _P, _D, _I, _P, _P, _P]),

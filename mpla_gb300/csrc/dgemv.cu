@@ -9,6 +9,8 @@
 //   * warp partials are summed in shared memory in warp order, and chunk
 //     partials across the grid by the last-arriving CTA of each strip in
 //     chunk order — a fixed summation order, so results are bit-reproducible.
+#include <mutex>
+
 #include "internal.h"
 #include "devutil.cuh"
 
@@ -142,6 +144,17 @@ __global__ void __launch_bounds__(kThreads) dgemv_kernel(int m, int n, const dou
   }
 }
 
+// ---------------------------------------------------------------------------
+// Scratch of the allocation-free entry point mgb_dgemv_noalloc: the split-K
+// partials and the per-strip arrival tickets live in this fixed array, which
+// every GPU that loads the library keeps for the life of the process.
+constexpr size_t kNoAllocPartials = size_t(1) << 20;  // doubles (8 MiB)
+constexpr int kNoAllocTickets = 16384;                // strips + 1
+constexpr int kNoAllocMaxChunkCols = 4096;            // 8 warps x 512 columns per CTA
+constexpr size_t kNoAllocBytes =
+    sizeof(double) * kNoAllocPartials + sizeof(unsigned int) * (kNoAllocTickets + 64);
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
 }  // namespace
 
 int launch_dgemv(DeviceContext* c, int m, int n, const double* A, int lda, const double* x,
@@ -182,3 +195,87 @@ int launch_dgemv(DeviceContext* c, int m, int n, const double* A, int lda, const
 }
 
 }  // namespace mgb
+
+using namespace mgb;
+
+namespace {
+
+// Per-device address of g_noalloc_scratch and SM count, resolved once per
+// device with that device current.  In host code the array's name is only a
+// host-side stand-in, never a device address.
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[64] = {nullptr};
+int g_noalloc_sms[64] = {0};
+
+int noalloc_setup(int dev, unsigned char** scratch, int* sms) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    MGB_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    int count = 0;
+    MGB_CUDA(cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev));
+    g_noalloc_sms[dev] = count;
+    g_noalloc_ptr[dev] = p;
+  }
+  *scratch = static_cast<unsigned char*>(g_noalloc_ptr[dev]);
+  *sms = g_noalloc_sms[dev];
+  return MGB_OK;
+}
+
+}  // namespace
+
+extern "C" int mgb_dgemv_noalloc(int m, int n, const double* A, int lda, const double* x, double* y, void* stream) {
+  if (m < 0 || n < 0 || lda < (m > 1 ? m : 1))
+    return set_error(MGB_ERR_ARG, "dgemv_noalloc: bad sizes m=%d n=%d lda=%d", m, n, lda);
+  if (m > 0 && n > 0 && (!A || !x || !y)) return set_error(MGB_ERR_ARG, "dgemv_noalloc: null pointer");
+  const bool vec2 = ((lda & 1) == 0) && ((reinterpret_cast<uintptr_t>(A) & 15) == 0);
+  const int rows_per_strip = vec2 ? 64 : 32;
+  const long long strips = ((long long)m + rows_per_strip - 1) / rows_per_strip;
+  if (strips + 1 > kNoAllocTickets)
+    return set_error(MGB_ERR_ARG, "dgemv_noalloc: m=%d exceeds the allocation-free maximum of %d rows", m,
+                     (kNoAllocTickets - 1) * rows_per_strip);
+  const long long min_split = ((long long)n + kNoAllocMaxChunkCols - 1) / kNoAllocMaxChunkCols;
+  if (min_split > 1 && min_split * m > (long long)kNoAllocPartials)
+    return set_error(MGB_ERR_ARG,
+                     "dgemv_noalloc: m x ceil(n/%d) = %lld exceeds the allocation-free scratch of %zu partials",
+                     kNoAllocMaxChunkCols, min_split * m, kNoAllocPartials);
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : cudaStreamLegacy;
+  if (m == 0) return MGB_OK;
+  if (n == 0) {
+    MGB_CUDA(cudaMemsetAsync(y, 0, sizeof(double) * m, s));
+    return MGB_OK;
+  }
+  int dev = 0;
+  MGB_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return set_error(MGB_ERR_ARG, "device index %d out of range", dev);
+  unsigned char* scratch = nullptr;
+  int sms = 0;
+  MGB_TRY(noalloc_setup(dev, &scratch, &sms));
+  double* partials = reinterpret_cast<double*>(scratch);
+  unsigned int* tickets = reinterpret_cast<unsigned int*>(scratch + sizeof(double) * kNoAllocPartials);
+  unsigned int* err = tickets + kNoAllocTickets;
+  // same column split as the allocating path, bounded by the fixed scratch
+  int cpw = 128;
+  const long long target = 6LL * sms;
+  while (cpw > 16 && strips * ((n + kWarps * cpw - 1) / (kWarps * cpw)) < target) cpw >>= 1;
+  while ((long long)((n + kWarps * cpw - 1) / (kWarps * cpw)) * m > (long long)kNoAllocPartials &&
+         kWarps * cpw < kNoAllocMaxChunkCols)
+    cpw <<= 1;
+  const int nsplit = (n + kWarps * cpw - 1) / (kWarps * cpw);
+  // The array keeps the previous call's contents: the arrival tickets must
+  // start at zero (the partials are written before they are read).
+  MGB_CUDA(cudaMemsetAsync(tickets, 0, sizeof(unsigned int) * (strips + 1), s));
+  const size_t smem = 16 + sizeof(double) * (kWarps * cpw + kWarps * rows_per_strip);
+  if (smem > 48 * 1024) return set_error(MGB_ERR_ARG, "dgemv_noalloc: column chunk too large");
+  const long long grid = strips * nsplit;
+  if (vec2) {
+    dgemv_kernel<2><<<(unsigned)grid, kThreads, smem, s>>>(m, n, A, lda, x, y, cpw, nsplit, partials, tickets + 1,
+                                                         nullptr, err);
+  } else {
+    dgemv_kernel<1><<<(unsigned)grid, kThreads, smem, s>>>(m, n, A, lda, x, y, cpw, nsplit, partials, tickets + 1,
+                                                         nullptr, err);
+  }
+  count_launches(1);
+  MGB_CUDA(cudaGetLastError());
+  return MGB_OK;
+}
