@@ -165,6 +165,35 @@ int mgb_time_gauss_matvec(int n, int dim, const double* const* coords_dev, doubl
 int mgb_time_dgemv(int n, const double* A_dev, const double* x_dev, double* y_dev, int reps,
                    double* ms_per_launch, void* stream);
 
+/* ------------------------------------------------ batched multi-system CG */
+/* Many independent Gaussian kernel systems, each with 1..8 right-hand sides,
+ * advanced together by one graph-captured step.  No counterpart in the
+ * reference: MPLA solves one system per call (mpla.cpp:888-1010); each
+ * right-hand side here runs that same CG iteration on its own scalars. */
+typedef struct mgb_batch mgb_batch;
+/* A batch with room for `max_systems` systems resident at once. */
+int mgb_batch_create(int max_systems, mgb_batch** out);
+/* Admit a system: n points of dimension 2 or 3 (structure of arrays,
+ * scaled so that K_ij = exp(-|x_i - x_j|^2) + nugget delta_ij), nrhs columns
+ * of b (column-major, n x nrhs) in host memory, x0 = 0.  Refused with
+ * MGB_ERR_NOMEM when its buffers plus `reserve_bytes` do not fit in free
+ * device memory or every slot is taken.  Returns a handle. */
+int mgb_batch_add(mgb_batch* b, int n, int dim, const double* coords_host, double nugget, int nrhs,
+                  const double* b_host, int precision, double eps, int iter_max, size_t reserve_bytes,
+                  int* handle);
+/* Advance every admitted system by up to max_steps iterations (whole
+ * graph replays); *active = systems with a right-hand side still running. */
+int mgb_batch_run(mgb_batch* b, int max_steps, int* active);
+/* Handles of systems whose right-hand sides have all finished. */
+int mgb_batch_finished(mgb_batch* b, int* handles, int capacity, int* count);
+/* Copy x (column-major, n x nrhs) and one mgb_solve_info per right-hand side
+ * to the host; release != 0 frees the slot and its device memory. */
+int mgb_batch_result(mgb_batch* b, int handle, double* x_host, mgb_solve_info* info, int release);
+/* Autotuner choice per (dimension, padded right-hand sides) class:
+ * rows_per_thread[8] and the timed ms of the 1/2/4 variants (ms[24]). */
+int mgb_batch_tuning(mgb_batch* b, int* rows_per_thread, float* ms);
+int mgb_batch_destroy(mgb_batch* b);
+
 /* ---------------------------------------------------------- checkpoint I/O */
 /* File format of mpla_save_vector (mpla.cpp:605-652): int32 n, then n float64. */
 int mgb_save_vector(const char* path, int n, const double* x_dev);

@@ -43,6 +43,8 @@ C_ABI_SYMBOLS = (
     "mgb_cg_dense", "mgb_bicgstab_dense", "mgb_cg_gauss", "mgb_bicgstab_gauss", "mgb_cg_gauss_host",
     "mgb_kernel_launches", "mgb_time_gauss_matvec", "mgb_time_dgemv",
     "mgb_save_vector", "mgb_load_vector",
+    "mgb_batch_create", "mgb_batch_add", "mgb_batch_run", "mgb_batch_finished", "mgb_batch_result",
+    "mgb_batch_tuning", "mgb_batch_destroy",
 )
 
 
@@ -103,6 +105,13 @@ _SIGS = {
     "mgb_time_dgemv": (_I, [_I, _P, _P, _P, _I, C.POINTER(_D), _P]),
     "mgb_save_vector": (_I, [C.c_char_p, _I, _P]),
     "mgb_load_vector": (_I, [C.c_char_p, _I, _P]),
+    "mgb_batch_create": (_I, [_I, C.POINTER(_P)]),
+    "mgb_batch_add": (_I, [_P, _I, _I, _P, _D, _I, _P, _I, _D, _I, C.c_size_t, C.POINTER(_I)]),
+    "mgb_batch_run": (_I, [_P, _I, C.POINTER(_I)]),
+    "mgb_batch_finished": (_I, [_P, _P, _I, C.POINTER(_I)]),
+    "mgb_batch_result": (_I, [_P, _I, _P, C.POINTER(SolveInfo), _I]),
+    "mgb_batch_tuning": (_I, [_P, _P, _P]),
+    "mgb_batch_destroy": (_I, [_P]),
 }
 
 
@@ -312,3 +321,72 @@ def cg_gauss_host(scaled_points: np.ndarray, nugget: float, b: np.ndarray, x0: n
                                  eps, precision, C.byref(info))
     _solve(st, info, allow_notconv)
     return x, info
+
+
+# ---------------------------------------------------------------- batching
+class Batch:
+    """Many independent Gaussian kernel systems (1..8 right-hand sides each)
+    advanced together on the device; see ``mgb_batch_*`` in mpla_gb300.h."""
+
+    def __init__(self, max_systems: int = 512):
+        h = _P()
+        check(lib().mgb_batch_create(int(max_systems), C.byref(h)))
+        self._h = h
+        self.max_systems = int(max_systems)
+
+    def add(self, scaled_points: np.ndarray, nugget: float, b: np.ndarray, precision: int = PREC_MIXED,
+            eps: float = 1e-10, iter_max: int = 200000, reserve_bytes: int = 0) -> int:
+        """Admit one system; ``scaled_points`` is dim x n (K_ij = exp(-|x_i-x_j|^2)),
+        ``b`` is n or n x nrhs.  Raises MplaError(MGB_ERR_NOMEM) when refused."""
+        pts = np.ascontiguousarray(scaled_points, dtype=np.float64)
+        dim, n = pts.shape
+        bb = np.asarray(b, dtype=np.float64)
+        if bb.ndim == 1:
+            bb = bb[:, None]
+        if bb.shape[0] != n:
+            raise ValueError("b must have one row per point")
+        bcol = np.asfortranarray(bb)
+        out = _I()
+        check(lib().mgb_batch_add(self._h, n, dim, pts.ctypes.data, float(nugget), bb.shape[1], bcol.ctypes.data,
+                                  int(precision), float(eps), int(iter_max), int(reserve_bytes), C.byref(out)))
+        return out.value
+
+    def run(self, max_steps: int = 1 << 30) -> int:
+        """Advance every system by up to ``max_steps`` iterations; returns the
+        number of systems still running."""
+        act = _I()
+        check(lib().mgb_batch_run(self._h, int(min(max_steps, 2**31 - 1)), C.byref(act)))
+        return act.value
+
+    def finished(self) -> list[int]:
+        buf = (_I * self.max_systems)()
+        cnt = _I()
+        check(lib().mgb_batch_finished(self._h, buf, self.max_systems, C.byref(cnt)))
+        return [buf[i] for i in range(cnt.value)]
+
+    def result(self, handle: int, n: int, nrhs: int, release: bool = True):
+        """x (n x nrhs) and a SolveInfo per right-hand side.  A right-hand side
+        that did not converge is reported in its SolveInfo, not raised."""
+        x = np.zeros((nrhs, n))
+        infos = (SolveInfo * nrhs)()
+        st = lib().mgb_batch_result(self._h, int(handle), x.ctypes.data, infos, int(bool(release)))
+        if st not in (MGB_OK, MGB_ERR_NOTCONV, MGB_ERR_BREAKDOWN):
+            check(st)
+        return x.T.copy(), list(infos)
+
+    def tuning(self):
+        rpt = (_I * 8)()
+        ms = (C.c_float * 24)()
+        check(lib().mgb_batch_tuning(self._h, rpt, ms))
+        return list(rpt), [list(ms[3 * c:3 * c + 3]) for c in range(8)]
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().mgb_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001 - interpreter shutdown
+            pass

@@ -1,0 +1,940 @@
+// Batched Gaussian-kernel CG: many independent systems, each with several
+// right-hand sides, advanced together by one graph-captured step.
+//
+// A "lane" is one right-hand side of one system: its own CG (the iteration of
+// mpla_generic_conjugate_gradient, mpla.cpp:888-1010) with its own scalars.
+// Vectors of a system are stored interleaved, element (i, k) of the n x R
+// block at i*R + k, so a matvec reads the R values of a point together and
+// reuses every kernel entry for all R lanes.
+//
+// One step (captured once into a CUDA graph, replayed until every lane is
+// done):
+//   mv32    persistent kernel over (system, 128-row tile) items of mixed
+//           systems: z = K~ d, entries in FP32 with the exponential on the
+//           SFU, 128-column partial sums in FP32 added into FP64
+//   mv64    persistent kernel over items of FP64 systems: z = K d in FP64
+//   alpha   one CTA per system: alpha_k = <r,r>_k / <d,z>_k
+//   update  one CTA per system: x += alpha d, r -= alpha z, new <r,r>; mixed
+//           lanes decide whether the FP64 true residual is due
+//   mv64r   persistent kernel over items of mixed systems with a pending
+//           replacement: z = K x in FP64 (returns at once otherwise)
+//   replace one CTA per system: r = b - z for those lanes, convergence test
+//           on the FP64 true residual, restart of the direction
+//   dir     one CTA per system: d = beta d + r (and its FP32 copy)
+// Systems and item lists live in device memory, so systems are added and
+// retired between replays (the serving loop) without re-capturing.
+//
+// Mixed precision.  K~ is the FP32 operator: coordinates are carried as an
+// FP32 pair (hi, lo) so that a coordinate difference is accurate to FP32
+// rounding of the difference itself (not of the coordinates), and K~ is
+// exactly symmetric.  The outer iteration is iterative refinement with
+// reliable residual replacement: when the recursive residual has fallen
+// 100x since the last FP64 true residual, when it claims convergence, or at
+// the iteration cap, r = b - K x in FP64 replaces it and the search
+// direction restarts from r (the FP32 operator's perturbation makes the old
+// direction's conjugacy unusable once r jumps).  Convergence is declared only
+// on the FP64 true residual.
+//
+// Rows per thread of the FP32 matvec (1, 2 or 4) are chosen per (dim, R)
+// class by timing each variant on the class's items at first use.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "internal.h"
+#include "devutil.cuh"
+#include "batch.h"
+
+namespace mgb {
+
+namespace {
+
+constexpr int kTile = 128;        // rows per item and threads per matvec CTA
+constexpr int kColTile = 128;     // columns staged per shared-memory round
+constexpr int kVecThreads = 256;  // per-system vector kernels
+
+enum LaneDone : int { LANE_RUNNING = 0, LANE_CONVERGED = 1, LANE_CAPPED = 2, LANE_BROKE = 3 };
+enum QueueMode : int { Q_MV32 = 0, Q_MV64 = 1, Q_MV64_TRUE = 2 };
+
+__device__ __forceinline__ float ex2_approx(float v) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(v));
+  return r;
+}
+
+__device__ __forceinline__ bool sys_active(const BatchSys& s) { return s.in_use && s.active_lanes > 0; }
+
+// Persistent work loop shared by the matvec kernels: items are claimed with
+// an atomic counter that the last CTA to finish resets for the next launch.
+struct WorkQueue {
+  const BatchItem* items;
+  const int* count;
+  int* counter;
+  unsigned int* finished;
+};
+
+__device__ __forceinline__ int claim(const WorkQueue& q, int* s_item) {
+  __syncthreads();
+  if (threadIdx.x == 0) *s_item = atomicAdd(q.counter, 1);
+  __syncthreads();
+  return *s_item;
+}
+
+__device__ __forceinline__ void queue_done(const WorkQueue& q) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned int prev = atomicAdd(q.finished, 1u);
+    if (prev == gridDim.x - 1) {
+      *q.counter = 0;
+      *q.finished = 0u;
+      __threadfence();
+    }
+  }
+}
+
+// ------------------------------------------------------- FP32 matvec
+// z = K~ d + nugget d for the R lanes of mixed systems of one class.
+template <int DIM, int R, int RPT>
+__global__ void __launch_bounds__(kTile) k_bmv32(WorkQueue q, const BatchSys* __restrict__ sys) {
+  __shared__ float4 sh[kColTile];
+  __shared__ float4 sl[kColTile];
+  __shared__ float sd[kColTile * R];
+  __shared__ int s_item;
+  for (;;) {
+    const int it = claim(q, &s_item);
+    if (it >= *q.count) break;
+    const BatchItem w = q.items[it];
+    const BatchSys& S = sys[w.sys];
+    if (!sys_active(S) || S.precision != MGB_PREC_MIXED || S.dim != DIM || S.R != R) continue;
+    // items are 128-row tiles; a variant with RPT rows per thread covers
+    // RPT consecutive tiles and takes only every RPT-th item
+    if ((w.row0 / kTile) % RPT != 0) continue;
+    const int n = S.n;
+    float4 hi[RPT], lo[RPT];
+    int row[RPT];
+#pragma unroll
+    for (int a = 0; a < RPT; ++a) {
+      row[a] = w.row0 + threadIdx.x + kTile * a;
+      hi[a] = S.pts_hi[min(row[a], n - 1)];
+      lo[a] = S.pts_lo[min(row[a], n - 1)];
+    }
+    double acc[RPT][R];
+#pragma unroll
+    for (int a = 0; a < RPT; ++a)
+#pragma unroll
+      for (int k = 0; k < R; ++k) acc[a][k] = 0.0;
+    for (int j0 = 0; j0 < n; j0 += kColTile) {
+      const int nj = min(kColTile, n - j0);
+      __syncthreads();
+      for (int t = threadIdx.x; t < kColTile; t += kTile) {
+        const bool in = t < nj;
+        sh[t] = in ? S.pts_hi[j0 + t] : make_float4(0.f, 0.f, 0.f, 0.f);
+        sl[t] = in ? S.pts_lo[j0 + t] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < R; ++k) sd[t * R + k] = in ? S.d32[(long long)(j0 + t) * R + k] : 0.f;
+      }
+      __syncthreads();
+      float part[RPT][R];
+#pragma unroll
+      for (int a = 0; a < RPT; ++a)
+#pragma unroll
+        for (int k = 0; k < R; ++k) part[a][k] = 0.f;
+#pragma unroll 2
+      for (int t = 0; t < nj; ++t) {
+        const float4 ph = sh[t];
+        const float4 pl = sl[t];
+        float dv[R];
+#pragma unroll
+        for (int k = 0; k < R; ++k) dv[k] = sd[t * R + k];
+#pragma unroll
+        for (int a = 0; a < RPT; ++a) {
+          const float dx = (hi[a].x - ph.x) + (lo[a].x - pl.x);
+          const float dy = (hi[a].y - ph.y) + (lo[a].y - pl.y);
+          float ns;
+          if (DIM == 2) {
+            ns = fmaf(-dx, dx, -dy * dy);
+          } else {
+            const float dz = (hi[a].z - ph.z) + (lo[a].z - pl.z);
+            ns = fmaf(-dx, dx, fmaf(-dy, dy, -dz * dz));
+          }
+          const float e = ex2_approx(ns);
+#pragma unroll
+          for (int k = 0; k < R; ++k) part[a][k] = fmaf(e, dv[k], part[a][k]);
+        }
+      }
+#pragma unroll
+      for (int a = 0; a < RPT; ++a)
+#pragma unroll
+        for (int k = 0; k < R; ++k) acc[a][k] += (double)part[a][k];
+    }
+#pragma unroll
+    for (int a = 0; a < RPT; ++a) {
+      if (row[a] < n) {
+#pragma unroll
+        for (int k = 0; k < R; ++k) {
+          const long long o = (long long)row[a] * R + k;
+          S.z[o] = fma(S.nugget, S.d[o], acc[a][k]);
+        }
+      }
+    }
+  }
+  queue_done(q);
+}
+
+// ------------------------------------------------------- FP64 matvec
+// mode Q_MV64: z = K d for FP64 systems; mode Q_MV64_TRUE: z = K x for mixed
+// systems with a pending true-residual replacement.
+template <int DIM, int R>
+__global__ void __launch_bounds__(kTile) k_bmv64(WorkQueue q, const BatchSys* __restrict__ sys, int mode,
+                                                 const double* __restrict__ table_g) {
+  __shared__ double table[kExpTableSize];
+  __shared__ double sp[DIM][kColTile];
+  __shared__ double sv[kColTile * R];
+  __shared__ int s_item;
+  for (int i = threadIdx.x; i < kExpTableSize; i += kTile) table[i] = table_g[i];
+  for (;;) {
+    const int it = claim(q, &s_item);
+    if (it >= *q.count) break;
+    const BatchItem w = q.items[it];
+    const BatchSys& S = sys[w.sys];
+    if (!sys_active(S) || S.dim != DIM || S.R != R) continue;
+    if (mode == Q_MV64 && S.precision != MGB_PREC_FP64) continue;
+    if (mode == Q_MV64_TRUE && (S.precision != MGB_PREC_MIXED || !S.need_hi)) continue;
+    const int n = S.n;
+    const double* v = mode == Q_MV64 ? S.d : S.x;
+    const int i = w.row0 + threadIdx.x;
+    double pi[DIM];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) pi[d] = S.pts64[(long long)d * n + min(i, n - 1)];
+    double acc[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) acc[k] = 0.0;
+    for (int j0 = 0; j0 < n; j0 += kColTile) {
+      const int nj = min(kColTile, n - j0);
+      __syncthreads();
+      for (int t = threadIdx.x; t < kColTile; t += kTile) {
+        const bool in = t < nj;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) sp[d][t] = in ? S.pts64[(long long)d * n + j0 + t] : 0.0;
+#pragma unroll
+        for (int k = 0; k < R; ++k) sv[t * R + k] = in ? v[(long long)(j0 + t) * R + k] : 0.0;
+      }
+      __syncthreads();
+      for (int t = 0; t < nj; ++t) {
+        double s = 0.0;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          const double df = pi[d] - sp[d][t];
+          s = (d == 0) ? df * df : fma(df, df, s);
+        }
+        const double e = exp_neg_table(s, table);
+#pragma unroll
+        for (int k = 0; k < R; ++k) acc[k] = fma(e, sv[t * R + k], acc[k]);
+      }
+    }
+    if (i < n) {
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        const long long o = (long long)i * R + k;
+        S.z[o] = fma(S.nugget, v[o], acc[k]);
+      }
+    }
+  }
+  queue_done(q);
+}
+
+// ---------------------------------------------------- per-system kernels
+// Block-wide sums of R per-thread values (one per lane); every thread gets
+// the totals.  Fixed order, so results do not depend on other systems.
+template <int R>
+__device__ __forceinline__ void block_sums(double (&v)[R], double* smem) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < R; ++k) v[k] = warp_sum(v[k]);
+  __syncthreads();
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < R; ++k) smem[warp * 8 + k] = v[k];
+  __syncthreads();
+  if (threadIdx.x < 32) {
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      double t = threadIdx.x < (kVecThreads >> 5) ? smem[threadIdx.x * 8 + k] : 0.0;
+      t = warp_sum(t);
+      if (threadIdx.x == 0) smem[64 + k] = t;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < R; ++k) v[k] = smem[64 + k];
+  __syncthreads();
+}
+
+template <int R>
+__device__ void vec_alpha(BatchSys& S, double* smem) {
+  double v[R];
+#pragma unroll
+  for (int k = 0; k < R; ++k) v[k] = 0.0;
+  for (int i = threadIdx.x; i < S.n; i += kVecThreads)
+#pragma unroll
+    for (int k = 0; k < R; ++k) v[k] = fma(S.d[(long long)i * R + k], S.z[(long long)i * R + k], v[k]);
+  block_sums<R>(v, smem);
+  if (threadIdx.x < R) {
+    BatchLane& L = S.lanes[threadIdx.x];
+    if (L.done == LANE_RUNNING) {
+      const double a = L.rr / v[threadIdx.x];
+      if (!(v[threadIdx.x] > 0.0) || !isfinite(a)) L.done = LANE_BROKE;
+      else L.alpha = a;
+    }
+  }
+}
+
+template <int R>
+__device__ void vec_update(BatchSys& S, double* smem, double delta2) {
+  __shared__ double s_alpha[8];
+  __shared__ int s_run[8];
+  if (threadIdx.x < R) {
+    s_alpha[threadIdx.x] = S.lanes[threadIdx.x].alpha;
+    s_run[threadIdx.x] = S.lanes[threadIdx.x].done == LANE_RUNNING;
+  }
+  __syncthreads();
+  double v[R];
+#pragma unroll
+  for (int k = 0; k < R; ++k) v[k] = 0.0;
+  for (int i = threadIdx.x; i < S.n; i += kVecThreads) {
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      const long long o = (long long)i * R + k;
+      if (s_run[k]) {
+        S.x[o] = fma(s_alpha[k], S.d[o], S.x[o]);
+        const double ri = fma(-s_alpha[k], S.z[o], S.r[o]);
+        S.r[o] = ri;
+        v[k] = fma(ri, ri, v[k]);
+      }
+    }
+  }
+  block_sums<R>(v, smem);
+  if (threadIdx.x == 0) {
+    int need = 0;
+    for (int k = 0; k < R; ++k) {
+      BatchLane& L = S.lanes[k];
+      if (L.done != LANE_RUNNING) continue;
+      L.k += 1;
+      const double rr_new = v[k];
+      if (S.precision == MGB_PREC_MIXED) {
+        const bool replace = (rr_new < delta2 * L.rr_ref) || (sqrt(rr_new) / L.bnorm < S.eps) ||
+                             (L.k + 1 >= S.iter_max) || !(rr_new == rr_new);
+        L.rr_new = rr_new;
+        L.flag = replace ? 1 : 0;
+        if (replace) {
+          need = 1;
+        } else {
+          L.beta = rr_new / L.rr;
+          L.rr = rr_new;
+        }
+      } else {
+        L.beta = rr_new / L.rr;
+        L.rr = rr_new;
+        L.res = sqrt(rr_new) / L.bnorm;
+        if (L.res < S.eps) L.done = LANE_CONVERGED;
+        else if (!(L.res == L.res)) L.done = LANE_BROKE;
+        else if (L.k + 1 >= S.iter_max) L.done = LANE_CAPPED;
+      }
+    }
+    S.need_hi = need;
+  }
+}
+
+template <int R>
+__device__ void vec_replace(BatchSys& S, double* smem) {
+  if (S.precision != MGB_PREC_MIXED || !S.need_hi) return;
+  __shared__ int s_flag[8];
+  if (threadIdx.x < R) s_flag[threadIdx.x] = S.lanes[threadIdx.x].done == LANE_RUNNING && S.lanes[threadIdx.x].flag;
+  __syncthreads();
+  double v[R];
+#pragma unroll
+  for (int k = 0; k < R; ++k) v[k] = 0.0;
+  for (int i = threadIdx.x; i < S.n; i += kVecThreads) {
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      if (!s_flag[k]) continue;
+      const long long o = (long long)i * R + k;
+      const double ri = S.b[o] - S.z[o];
+      S.r[o] = ri;
+      v[k] = fma(ri, ri, v[k]);
+    }
+  }
+  block_sums<R>(v, smem);
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < R; ++k) {
+      if (!s_flag[k]) continue;
+      BatchLane& L = S.lanes[k];
+      L.res = sqrt(v[k]) / L.bnorm;
+      L.replacements += 1;
+      L.beta = 0.0;  // restart the direction from the true residual
+      L.rr = v[k];
+      L.rr_ref = v[k];
+      L.flag = 0;
+      if (L.res < S.eps) L.done = LANE_CONVERGED;
+      else if (!(L.res == L.res)) L.done = LANE_BROKE;
+      else if (L.k + 1 >= S.iter_max) L.done = LANE_CAPPED;
+    }
+    S.need_hi = 0;
+  }
+}
+
+template <int R>
+__device__ void vec_direction(BatchSys& S) {
+  __shared__ double s_beta[8];
+  __shared__ int s_run[8];
+  if (threadIdx.x < R) {
+    s_beta[threadIdx.x] = S.lanes[threadIdx.x].beta;
+    s_run[threadIdx.x] = S.lanes[threadIdx.x].done == LANE_RUNNING;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < S.n; i += kVecThreads) {
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      const long long o = (long long)i * R + k;
+      const double dn = s_run[k] ? __dadd_rn(__dmul_rn(s_beta[k], S.d[o]), S.r[o]) : 0.0;
+      S.d[o] = dn;
+      if (S.d32) S.d32[o] = (float)dn;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int act = 0;
+    for (int k = 0; k < R; ++k) act += S.lanes[k].done == LANE_RUNNING;
+    S.active_lanes = act;
+  }
+}
+
+// One kernel per phase, one CTA per system slot; the R dispatch is a
+// runtime switch over templated bodies.
+template <int PHASE>
+__global__ void __launch_bounds__(kVecThreads) k_bvec(BatchSys* sys, int nslots, double delta2) {
+  __shared__ double smem[80];
+  const int sidx = blockIdx.x;
+  if (sidx >= nslots) return;
+  BatchSys& S = sys[sidx];
+  if (!sys_active(S)) return;
+  switch (S.R) {
+#define MGB_BVEC_CASE(RR)                            \
+  case RR:                                           \
+    if (PHASE == 0) vec_alpha<RR>(S, smem);          \
+    if (PHASE == 1) vec_update<RR>(S, smem, delta2); \
+    if (PHASE == 2) vec_replace<RR>(S, smem);        \
+    if (PHASE == 3) vec_direction<RR>(S);            \
+    break;
+    MGB_BVEC_CASE(1)
+    MGB_BVEC_CASE(2)
+    MGB_BVEC_CASE(4)
+    MGB_BVEC_CASE(8)
+#undef MGB_BVEC_CASE
+    default:
+      break;
+  }
+}
+
+// Initial state with x0 = 0: r = d = b, <r,r> and ||b|| per lane.
+__global__ void __launch_bounds__(kVecThreads) k_binit(BatchSys* sys, int slot) {
+  __shared__ double smem[80];
+  BatchSys& S = sys[slot];
+  const int R = S.R;
+  double v[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) v[k] = 0.0;
+  for (int i = threadIdx.x; i < S.n; i += kVecThreads)
+    for (int k = 0; k < R; ++k) {
+      const long long o = (long long)i * R + k;
+      const double bv = S.b[o];
+      S.x[o] = 0.0;
+      S.r[o] = bv;
+      S.d[o] = bv;
+      if (S.d32) S.d32[o] = (float)bv;
+      v[k] = fma(bv, bv, v[k]);
+    }
+  block_sums<8>(v, smem);
+  if (threadIdx.x == 0) {
+    int act = 0;
+    for (int k = 0; k < 8; ++k) {
+      BatchLane& L = S.lanes[k];
+      L = BatchLane{};
+      L.rr = v[k];
+      L.rr_ref = v[k];
+      L.bnorm = sqrt(v[k]);
+      L.res = (L.bnorm > 0.0) ? 1.0 : 0.0;
+      if (k >= S.nrhs || L.bnorm == 0.0) L.done = LANE_CONVERGED;  // padding lanes and b = 0
+      else if (S.iter_max <= 1) L.done = LANE_CAPPED;
+      act += L.done == LANE_RUNNING;
+    }
+    S.active_lanes = act;
+    S.need_hi = 0;
+  }
+}
+
+__global__ void k_bcount(const BatchSys* sys, int nslots, int* active) {
+  __shared__ int sm[32];
+  int a = 0;
+  for (int s = threadIdx.x; s < nslots; s += blockDim.x) a += sys_active(sys[s]) ? 1 : 0;
+  a = __reduce_add_sync(0xffffffffu, a);
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = a;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sm[w];
+    *active = t;
+  }
+}
+
+int padded_rhs(int r) { return r <= 1 ? 1 : (r <= 2 ? 2 : (r <= 4 ? 4 : 8)); }
+
+}  // namespace
+
+// --------------------------------------------------------------- engine
+int BatchEngine::init(DeviceContext* c, int max_systems, cudaStream_t s) {
+  c_ = c;
+  s_ = s;
+  max_ = max_systems;
+  host_.assign(max_systems, BatchSys{});
+  blocks_.assign(max_systems, nullptr);
+  MGB_TRY(pool_alloc(c, sizeof(BatchSys) * max_systems, (void**)&dev_sys_));
+  MGB_CUDA(cudaMemsetAsync(dev_sys_, 0, sizeof(BatchSys) * max_systems, s));
+  max_items_ = 1 << 16;
+  for (int q = 0; q < kClasses; ++q) {
+    MGB_TRY(pool_alloc(c, sizeof(BatchItem) * max_items_, (void**)&items_[q]));
+    items_host_[q].clear();
+  }
+  MGB_TRY(pool_alloc(c, sizeof(int) * kCounterInts, (void**)&counters_));
+  MGB_CUDA(cudaMemsetAsync(counters_, 0, sizeof(int) * kCounterInts, s));
+  MGB_CUDA(cudaMallocHost(&active_host_, sizeof(int)));
+  for (int k = 0; k < kClasses; ++k) rpt_[k] = 0;
+  MGB_CUDA(cudaStreamSynchronize(s));
+  return MGB_OK;
+}
+
+BatchEngine::~BatchEngine() {
+  if (!c_) return;
+  cudaStreamSynchronize(s_);
+  for (int i = 0; i < max_; ++i)
+    if (host_[i].in_use) release_slot(i);
+  for (int q = 0; q < kClasses; ++q)
+    if (items_[q]) pool_free(c_, items_[q]);
+  if (counters_) pool_free(c_, counters_);
+  if (dev_sys_) pool_free(c_, dev_sys_);
+  if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+  if (graph_) cudaGraphDestroy(graph_);
+  if (active_host_) cudaFreeHost(active_host_);
+}
+
+int BatchEngine::class_of(int dim, int R) {
+  const int r = R == 1 ? 0 : (R == 2 ? 1 : (R == 4 ? 2 : 3));
+  return (dim == 2 ? 0 : 4) + r;
+}
+
+size_t BatchEngine::bytes_needed(int n, int dim, int nrhs, int precision) {
+  const int R = padded_rhs(nrhs);
+  const size_t nv = (size_t)n * R;
+  size_t b = 5 * (sizeof(double) * nv + 256) + sizeof(double) * (size_t)n * dim + 256 + sizeof(BatchLane) * 8 + 256;
+  if (precision == MGB_PREC_MIXED) b += 2 * (sizeof(float4) * (size_t)n + 256) + sizeof(float) * nv + 256;
+  return b;
+}
+
+int BatchEngine::add(int n, int dim, const double* coords_host, double nugget, int nrhs, const double* b_host,
+                     int precision, double eps, int iter_max, size_t reserve_bytes, int* handle) {
+  if (n <= 0 || (dim != 2 && dim != 3) || nrhs < 1 || nrhs > 8 || !coords_host || !b_host || iter_max < 1)
+    return set_error(MGB_ERR_ARG, "batch add: n > 0, dim in {2,3}, 1 <= nrhs <= 8, iter_max >= 1 required");
+  if (precision != MGB_PREC_FP64 && precision != MGB_PREC_MIXED)
+    return set_error(MGB_ERR_ARG, "batch add: unknown precision %d", precision);
+  int slot = -1;
+  for (int i = 0; i < max_; ++i)
+    if (!host_[i].in_use) {
+      slot = i;
+      break;
+    }
+  if (slot < 0) return set_error(MGB_ERR_NOMEM, "batch add: all %d system slots in use", max_);
+  const int R = padded_rhs(nrhs);
+  const int cls = class_of(dim, R);
+  const int new_items = (n + kTile - 1) / kTile;
+  if ((int)items_host_[cls].size() + new_items > max_items_)
+    return set_error(MGB_ERR_NOMEM, "batch add: more than %d work items in one class", max_items_);
+  // admission by free device memory
+  const size_t need = bytes_needed(n, dim, nrhs, precision);
+  size_t free_b = 0, total_b = 0;
+  MGB_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  if (reserve_bytes > free_b || need > free_b - reserve_bytes)
+    return set_error(MGB_ERR_NOMEM, "batch add: %zu bytes needed, %zu free (reserve %zu)", need, free_b,
+                     reserve_bytes);
+  BatchSys S{};
+  S.in_use = 1;
+  S.n = n;
+  S.dim = dim;
+  S.R = R;
+  S.nrhs = nrhs;
+  S.precision = precision;
+  S.iter_max = iter_max;
+  S.eps = eps;
+  S.nugget = nugget;
+  char* base = nullptr;
+  MGB_TRY(pool_alloc(c_, need, (void**)&base));
+  blocks_[slot] = base;
+  auto take = [&](size_t bytes) {
+    char* p = base;
+    base += (bytes + 255) & ~size_t(255);
+    return p;
+  };
+  const size_t nv = (size_t)n * R;
+  S.x = (double*)take(sizeof(double) * nv);
+  S.r = (double*)take(sizeof(double) * nv);
+  S.d = (double*)take(sizeof(double) * nv);
+  S.z = (double*)take(sizeof(double) * nv);
+  S.b = (double*)take(sizeof(double) * nv);
+  S.pts64 = (const double*)take(sizeof(double) * (size_t)n * dim);
+  S.lanes = (BatchLane*)take(sizeof(BatchLane) * 8);
+  if (precision == MGB_PREC_MIXED) {
+    S.pts_hi = (const float4*)take(sizeof(float4) * (size_t)n);
+    S.pts_lo = (const float4*)take(sizeof(float4) * (size_t)n);
+    S.d32 = (float*)take(sizeof(float) * nv);
+  }
+  // host staging: interleave b; split the scaled coordinates into FP32 pairs
+  std::vector<double> bh(nv, 0.0);
+  for (int k = 0; k < nrhs; ++k)
+    for (int i = 0; i < n; ++i) bh[(size_t)i * R + k] = b_host[(size_t)k * n + i];
+  MGB_CUDA(cudaMemcpyAsync(S.b, bh.data(), sizeof(double) * nv, cudaMemcpyHostToDevice, s_));
+  MGB_CUDA(cudaMemcpyAsync((void*)S.pts64, coords_host, sizeof(double) * (size_t)n * dim, cudaMemcpyHostToDevice,
+                           s_));
+  std::vector<float4> ph, pl;
+  if (precision == MGB_PREC_MIXED) {
+    ph.resize(n);
+    pl.resize(n);
+    const double sc = std::sqrt(1.4426950408889634);  // exp(-s) = 2^(-s log2 e)
+    for (int i = 0; i < n; ++i) {
+      float h[3] = {0.f, 0.f, 0.f}, l[3] = {0.f, 0.f, 0.f};
+      for (int d = 0; d < dim; ++d) {
+        const double v = coords_host[(size_t)d * n + i] * sc;
+        h[d] = (float)v;
+        l[d] = (float)(v - (double)h[d]);
+      }
+      ph[i] = make_float4(h[0], h[1], h[2], 0.f);
+      pl[i] = make_float4(l[0], l[1], l[2], 0.f);
+    }
+    MGB_CUDA(cudaMemcpyAsync((void*)S.pts_hi, ph.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s_));
+    MGB_CUDA(cudaMemcpyAsync((void*)S.pts_lo, pl.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s_));
+  }
+  host_[slot] = S;
+  MGB_CUDA(cudaMemcpyAsync(dev_sys_ + slot, &host_[slot], sizeof(BatchSys), cudaMemcpyHostToDevice, s_));
+  k_binit<<<1, kVecThreads, 0, s_>>>(dev_sys_, slot);
+  count_launches(1);
+  MGB_CUDA(cudaGetLastError());
+  // the host staging buffers must outlive the async copies
+  MGB_CUDA(cudaStreamSynchronize(s_));
+  for (int r0 = 0; r0 < n; r0 += kTile) items_host_[cls].push_back(BatchItem{slot, r0});
+  items_dirty_ = true;
+  nslots_ = std::max(nslots_, slot + 1);
+  *handle = slot;
+  return MGB_OK;
+}
+
+void BatchEngine::release_slot(int slot) {
+  pool_free(c_, blocks_[slot]);
+  blocks_[slot] = nullptr;
+  const int cls = class_of(host_[slot].dim, host_[slot].R);
+  auto& v = items_host_[cls];
+  v.erase(std::remove_if(v.begin(), v.end(), [&](const BatchItem& w) { return w.sys == slot; }), v.end());
+  host_[slot] = BatchSys{};
+  items_dirty_ = true;
+}
+
+int BatchEngine::sync_items() {
+  if (!items_dirty_) return MGB_OK;
+  for (int q = 0; q < kClasses; ++q) {
+    const int cnt = (int)items_host_[q].size();
+    if (cnt)
+      MGB_CUDA(cudaMemcpyAsync(items_[q], items_host_[q].data(), sizeof(BatchItem) * cnt, cudaMemcpyHostToDevice,
+                               s_));
+    count_host_[q] = cnt;
+  }
+  MGB_CUDA(cudaMemcpyAsync(counters_ + 6 * kClasses, count_host_, sizeof(int) * kClasses, cudaMemcpyHostToDevice,
+                           s_));
+  MGB_CUDA(cudaStreamSynchronize(s_));
+  items_dirty_ = false;
+  return MGB_OK;
+}
+
+// counters_ layout: [class][mode] -> (claim, finished) at (cls * 3 + mode) * 2,
+// item counts at 6 * kClasses + cls, active systems at 7 * kClasses.
+static WorkQueue make_queue(const BatchItem* items, int* counters, int cls, int mode, int classes) {
+  WorkQueue q;
+  q.items = items;
+  q.count = counters + 6 * classes + cls;
+  q.counter = counters + (cls * 3 + mode) * 2;
+  q.finished = reinterpret_cast<unsigned int*>(counters + (cls * 3 + mode) * 2 + 1);
+  return q;
+}
+
+template <int DIM, int R>
+static void launch_mv32(const WorkQueue& q, const BatchSys* sys, int rpt, int grid, cudaStream_t s) {
+  if (rpt == 4) k_bmv32<DIM, R, 4><<<grid, kTile, 0, s>>>(q, sys);
+  else if (rpt == 2) k_bmv32<DIM, R, 2><<<grid, kTile, 0, s>>>(q, sys);
+  else k_bmv32<DIM, R, 1><<<grid, kTile, 0, s>>>(q, sys);
+}
+
+int BatchEngine::enqueue_mv32(int cls, int rpt) {
+  const WorkQueue q = make_queue(items_[cls], counters_, cls, Q_MV32, kClasses);
+  const int grid = 4 * c_->num_sms;
+  switch (cls) {
+    case 0: launch_mv32<2, 1>(q, dev_sys_, rpt, grid, s_); break;
+    case 1: launch_mv32<2, 2>(q, dev_sys_, rpt, grid, s_); break;
+    case 2: launch_mv32<2, 4>(q, dev_sys_, rpt, grid, s_); break;
+    case 3: launch_mv32<2, 8>(q, dev_sys_, rpt, grid, s_); break;
+    case 4: launch_mv32<3, 1>(q, dev_sys_, rpt, grid, s_); break;
+    case 5: launch_mv32<3, 2>(q, dev_sys_, rpt, grid, s_); break;
+    case 6: launch_mv32<3, 4>(q, dev_sys_, rpt, grid, s_); break;
+    default: launch_mv32<3, 8>(q, dev_sys_, rpt, grid, s_); break;
+  }
+  count_launches(1);
+  MGB_CUDA(cudaGetLastError());
+  return MGB_OK;
+}
+
+int BatchEngine::enqueue_mv64(int cls, int mode) {
+  const WorkQueue q = make_queue(items_[cls], counters_, cls, mode, kClasses);
+  const int grid = 2 * c_->num_sms;
+  const double* t = c_->exp_table;
+  switch (cls) {
+    case 0: k_bmv64<2, 1><<<grid, kTile, 0, s_>>>(q, dev_sys_, mode, t); break;
+    case 1: k_bmv64<2, 2><<<grid, kTile, 0, s_>>>(q, dev_sys_, mode, t); break;
+    case 2: k_bmv64<2, 4><<<grid, kTile, 0, s_>>>(q, dev_sys_, mode, t); break;
+    case 3: k_bmv64<2, 8><<<grid, kTile, 0, s_>>>(q, dev_sys_, mode, t); break;
+    case 4: k_bmv64<3, 1><<<grid, kTile, 0, s_>>>(q, dev_sys_, mode, t); break;
+    case 5: k_bmv64<3, 2><<<grid, kTile, 0, s_>>>(q, dev_sys_, mode, t); break;
+    case 6: k_bmv64<3, 4><<<grid, kTile, 0, s_>>>(q, dev_sys_, mode, t); break;
+    default: k_bmv64<3, 8><<<grid, kTile, 0, s_>>>(q, dev_sys_, mode, t); break;
+  }
+  count_launches(1);
+  MGB_CUDA(cudaGetLastError());
+  return MGB_OK;
+}
+
+int BatchEngine::enqueue_step() {
+  const double delta2 = 1e-4;  // replacement when the recursive residual fell 100x
+  for (int cls = 0; cls < kClasses; ++cls) {
+    if (!count_host_[cls]) continue;
+    MGB_TRY(enqueue_mv32(cls, rpt_[cls] ? rpt_[cls] : 1));
+    MGB_TRY(enqueue_mv64(cls, Q_MV64));
+  }
+  k_bvec<0><<<nslots_, kVecThreads, 0, s_>>>(dev_sys_, nslots_, delta2);
+  k_bvec<1><<<nslots_, kVecThreads, 0, s_>>>(dev_sys_, nslots_, delta2);
+  count_launches(2);
+  for (int cls = 0; cls < kClasses; ++cls)
+    if (count_host_[cls]) MGB_TRY(enqueue_mv64(cls, Q_MV64_TRUE));
+  k_bvec<2><<<nslots_, kVecThreads, 0, s_>>>(dev_sys_, nslots_, delta2);
+  k_bvec<3><<<nslots_, kVecThreads, 0, s_>>>(dev_sys_, nslots_, delta2);
+  k_bcount<<<1, 256, 0, s_>>>(dev_sys_, nslots_, counters_ + 7 * kClasses);
+  count_launches(3);
+  MGB_CUDA(cudaGetLastError());
+  return MGB_OK;
+}
+
+// Autotuner: for each class with mixed work and no choice yet, time one FP32
+// matvec of each rows-per-thread variant (outside any capture; the matvec
+// only rewrites z, which every step recomputes) and keep the fastest.
+int BatchEngine::autotune() {
+  cudaEvent_t e0, e1;
+  MGB_CUDA(cudaEventCreate(&e0));
+  MGB_CUDA(cudaEventCreate(&e1));
+  int st = MGB_OK;
+  for (int cls = 0; cls < kClasses && st == MGB_OK; ++cls) {
+    if (!count_host_[cls] || rpt_[cls]) continue;
+    bool mixed = false;
+    for (const BatchItem& w : items_host_[cls]) mixed |= host_[w.sys].precision == MGB_PREC_MIXED;
+    if (!mixed) continue;
+    float best = 1e30f;
+    int best_rpt = 1;
+    for (int v = 0; v < 3 && st == MGB_OK; ++v) {
+      const int rpt = 1 << v;
+      st = enqueue_mv32(cls, rpt);  // warm-up
+      if (st != MGB_OK) break;
+      if (cudaEventRecord(e0, s_) != cudaSuccess) {
+        st = set_error(MGB_ERR_CUDA, "batch autotune: event failure");
+        break;
+      }
+      st = enqueue_mv32(cls, rpt);
+      if (st != MGB_OK) break;
+      if (cudaEventRecord(e1, s_) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
+        st = set_error(MGB_ERR_CUDA, "batch autotune: event failure");
+        break;
+      }
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      tune_ms_[cls][v] = ms;
+      if (ms < best) {
+        best = ms;
+        best_rpt = rpt;
+      }
+    }
+    rpt_[cls] = best_rpt;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return st;
+}
+
+int BatchEngine::run_steps(int steps, int* active_out) {
+  MGB_TRY(sync_items());
+  MGB_TRY(autotune());
+  // (re)capture when the set of non-empty classes, the slot range or a
+  // tuning choice changed
+  unsigned int sig = 0;
+  for (int q = 0; q < kClasses; ++q) sig |= (count_host_[q] ? 1u : 0u) << q;
+  sig |= (unsigned)nslots_ << 8;
+  for (int q = 0; q < kClasses; ++q) sig = sig * 31u + (unsigned)rpt_[q];
+  if (!graph_exec_ || sig != graph_sig_) {
+    if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+    if (graph_) cudaGraphDestroy(graph_);
+    graph_exec_ = nullptr;
+    graph_ = nullptr;
+    MGB_CUDA(cudaStreamBeginCapture(s_, cudaStreamCaptureModeThreadLocal));
+    begin_capture_count();
+    int st = MGB_OK;
+    for (int i = 0; i < kStepsPerGraph && st == MGB_OK; ++i) st = enqueue_step();
+    graph_kernels_ = end_capture_count();
+    cudaError_t e = cudaStreamEndCapture(s_, &graph_);
+    if (st != MGB_OK) return st;
+    if (e != cudaSuccess) return cuda_error(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+    MGB_CUDA(cudaGraphInstantiate(&graph_exec_, graph_, 0));
+    graph_sig_ = sig;
+  }
+  int done_steps = 0;
+  int active = 0;
+  for (int i = 0; i < nslots_; ++i) active += host_[i].in_use;
+  while (active > 0 && done_steps < steps) {
+    MGB_CUDA(cudaGraphLaunch(graph_exec_, s_));
+    count_launches(graph_kernels_);
+    done_steps += kStepsPerGraph;
+    MGB_CUDA(cudaMemcpyAsync(active_host_, counters_ + 7 * kClasses, sizeof(int), cudaMemcpyDeviceToHost, s_));
+    MGB_CUDA(cudaStreamSynchronize(s_));
+    active = *active_host_;
+  }
+  if (active_out) *active_out = active;
+  return MGB_OK;
+}
+
+int BatchEngine::result(int handle, double* x_host, mgb_solve_info* info, bool release) {
+  if (handle < 0 || handle >= max_ || !host_[handle].in_use)
+    return set_error(MGB_ERR_ARG, "bad batch handle %d", handle);
+  const BatchSys& H = host_[handle];
+  BatchLane lanes[8];
+  MGB_CUDA(cudaMemcpyAsync(lanes, H.lanes, sizeof(lanes), cudaMemcpyDeviceToHost, s_));
+  std::vector<double> xi((size_t)H.n * H.R);
+  MGB_CUDA(cudaMemcpyAsync(xi.data(), H.x, sizeof(double) * xi.size(), cudaMemcpyDeviceToHost, s_));
+  MGB_CUDA(cudaStreamSynchronize(s_));
+  if (x_host)
+    for (int k = 0; k < H.nrhs; ++k)
+      for (int i = 0; i < H.n; ++i) x_host[(size_t)k * H.n + i] = xi[(size_t)i * H.R + k];
+  int status = MGB_OK;
+  for (int k = 0; k < H.nrhs; ++k) {
+    const int st = lanes[k].done == LANE_CONVERGED ? MGB_OK
+                   : lanes[k].done == LANE_BROKE   ? MGB_ERR_BREAKDOWN
+                                                   : MGB_ERR_NOTCONV;
+    if (st != MGB_OK && status == MGB_OK) status = st;
+    if (!info) continue;
+    mgb_solve_info& f = info[k];
+    memset(&f, 0, sizeof(f));
+    f.iterations = lanes[k].k;
+    f.status = st;
+    f.final_res = lanes[k].res;
+    f.true_relres = H.precision == MGB_PREC_MIXED ? lanes[k].res : -1.0;
+    f.fp64_matvecs = H.precision == MGB_PREC_MIXED ? lanes[k].replacements : lanes[k].k;
+    f.low_matvecs = H.precision == MGB_PREC_MIXED ? lanes[k].k : 0;
+  }
+  if (release) {
+    BatchSys empty{};
+    MGB_CUDA(cudaMemcpyAsync(dev_sys_ + handle, &empty, sizeof(BatchSys), cudaMemcpyHostToDevice, s_));
+    MGB_CUDA(cudaStreamSynchronize(s_));
+    release_slot(handle);
+  }
+  if (status != MGB_OK) set_error(status, "batch system %d: a right-hand side did not converge", handle);
+  return status;
+}
+
+int BatchEngine::done_handles(std::vector<int>* out) {
+  out->clear();
+  if (nslots_ == 0) return MGB_OK;
+  std::vector<BatchSys> snap(nslots_);
+  MGB_CUDA(cudaMemcpyAsync(snap.data(), dev_sys_, sizeof(BatchSys) * nslots_, cudaMemcpyDeviceToHost, s_));
+  MGB_CUDA(cudaStreamSynchronize(s_));
+  for (int i = 0; i < nslots_; ++i)
+    if (host_[i].in_use && snap[i].active_lanes == 0) out->push_back(i);
+  return MGB_OK;
+}
+
+}  // namespace mgb
+
+// ------------------------------------------------------------------ C ABI
+struct mgb_batch {
+  mgb::BatchEngine engine;
+};
+
+using namespace mgb;
+
+extern "C" {
+
+int mgb_batch_create(int max_systems, mgb_batch** out) {
+  if (!out || max_systems <= 0) return set_error(MGB_ERR_ARG, "mgb_batch_create: bad arguments");
+  DeviceContext* c = nullptr;
+  MGB_TRY(context(&c));
+  mgb_batch* b = new mgb_batch();
+  const int st = b->engine.init(c, max_systems, c->stream);
+  if (st != MGB_OK) {
+    delete b;
+    return st;
+  }
+  *out = b;
+  return MGB_OK;
+}
+
+int mgb_batch_add(mgb_batch* b, int n, int dim, const double* coords_host, double nugget, int nrhs,
+                  const double* b_host, int precision, double eps, int iter_max, size_t reserve_bytes, int* handle) {
+  if (!b || !handle) return set_error(MGB_ERR_ARG, "mgb_batch_add: null argument");
+  return b->engine.add(n, dim, coords_host, nugget, nrhs, b_host, precision, eps, iter_max, reserve_bytes, handle);
+}
+
+int mgb_batch_run(mgb_batch* b, int max_steps, int* active) {
+  if (!b) return set_error(MGB_ERR_ARG, "mgb_batch_run: null batch");
+  return b->engine.run_steps(max_steps, active);
+}
+
+int mgb_batch_finished(mgb_batch* b, int* handles, int capacity, int* count) {
+  if (!b || !count || (capacity > 0 && !handles)) return set_error(MGB_ERR_ARG, "mgb_batch_finished: null argument");
+  std::vector<int> h;
+  MGB_TRY(b->engine.done_handles(&h));
+  const int m = (int)h.size() < capacity ? (int)h.size() : capacity;
+  for (int i = 0; i < m; ++i) handles[i] = h[i];
+  *count = m;
+  return MGB_OK;
+}
+
+int mgb_batch_result(mgb_batch* b, int handle, double* x_host, mgb_solve_info* info, int release) {
+  if (!b) return set_error(MGB_ERR_ARG, "mgb_batch_result: null batch");
+  return b->engine.result(handle, x_host, info, release != 0);
+}
+
+int mgb_batch_tuning(mgb_batch* b, int* rows_per_thread, float* ms) {
+  if (!b) return set_error(MGB_ERR_ARG, "mgb_batch_tuning: null batch");
+  for (int c = 0; c < BatchEngine::kClasses; ++c) {
+    if (rows_per_thread) rows_per_thread[c] = b->engine.rows_per_thread()[c];
+    if (ms)
+      for (int v = 0; v < 3; ++v) ms[3 * c + v] = b->engine.tune_ms(c)[v];
+  }
+  return MGB_OK;
+}
+
+int mgb_batch_destroy(mgb_batch* b) {
+  delete b;
+  return MGB_OK;
+}
+
+}  // extern "C"

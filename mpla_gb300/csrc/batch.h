@@ -1,0 +1,100 @@
+// Batched multi-system, multi-RHS Gaussian-kernel CG engine (internal).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <vector>
+
+#include "internal.h"
+
+namespace mgb {
+
+// CG scalars of one right-hand side ("lane") of one system.
+struct BatchLane {
+  double rr;        // <r,r> of the current (recursive) residual
+  double rr_new;    // <r,r> after this iteration's update (mixed lanes)
+  double rr_ref;    // <r,r> at the last FP64 true residual (mixed lanes)
+  double alpha, beta;
+  double bnorm;     // ||b||
+  double res;       // last stopping measure: ||r|| / ||b||
+  int k;            // iterations done
+  int done;         // 0 running, 1 converged, 2 capped, 3 broke down
+  int flag;         // mixed: FP64 true residual due this iteration
+  int replacements; // mixed: FP64 true residuals computed
+};
+
+// One system, resident in device memory.  Vectors are n x R interleaved
+// (element (i, k) at i * R + k); R is nrhs padded to 1, 2, 4 or 8.
+struct BatchSys {
+  int in_use;
+  int n, dim, R, nrhs;
+  int precision;     // MGB_PREC_FP64 or MGB_PREC_MIXED
+  int iter_max;
+  int active_lanes;  // lanes still running
+  int need_hi;       // mixed: some lane needs the FP64 true residual this step
+  int pad;
+  double eps, nugget;
+  double *x, *r, *d, *z, *b;
+  const double* pts64;   // dim x n, structure of arrays
+  const float4* pts_hi;  // mixed: coordinates x sqrt(log2 e), rounded to FP32 ...
+  const float4* pts_lo;  // ... and the FP32 remainder (hi + lo carries ~48 bits)
+  float* d32;            // mixed: FP32 copy of d
+  BatchLane* lanes;      // 8 lanes
+};
+
+// A work item of the persistent matvec kernels: 128 rows of one system.
+struct BatchItem {
+  int sys;
+  int row0;
+};
+
+class BatchEngine {
+ public:
+  static constexpr int kClasses = 8;        // (dim 2|3) x (R 1|2|4|8)
+  static constexpr int kStepsPerGraph = 8;  // CG iterations per graph replay
+  // counters: per class and mode, (claim counter, finished counter, pad);
+  // then the item counts per class; then the active-system count
+  static constexpr int kCounterInts = 6 * kClasses + kClasses + 4;
+
+  ~BatchEngine();
+  int init(DeviceContext* c, int max_systems, cudaStream_t s);
+  int add(int n, int dim, const double* coords_host, double nugget, int nrhs, const double* b_host,
+          int precision, double eps, int iter_max, size_t reserve_bytes, int* handle);
+  int run_steps(int steps, int* active_out);
+  int done_handles(std::vector<int>* out);
+  int result(int handle, double* x_host, mgb_solve_info* info, bool release);
+  const int* rows_per_thread() const { return rpt_; }
+  const float* tune_ms(int cls) const { return tune_ms_[cls]; }
+
+ private:
+  static int class_of(int dim, int R);
+  static size_t bytes_needed(int n, int dim, int nrhs, int precision);
+  void release_slot(int slot);
+  int sync_items();
+  int autotune();
+  int enqueue_step();
+  int enqueue_mv32(int cls, int rpt);
+  int enqueue_mv64(int cls, int mode);
+
+  DeviceContext* c_ = nullptr;
+  cudaStream_t s_ = nullptr;
+  int max_ = 0;
+  int nslots_ = 0;
+  std::vector<BatchSys> host_;
+  std::vector<void*> blocks_;
+  BatchSys* dev_sys_ = nullptr;
+  BatchItem* items_[kClasses] = {};
+  std::vector<BatchItem> items_host_[kClasses];
+  int count_host_[kClasses] = {};
+  int max_items_ = 0;
+  bool items_dirty_ = false;
+  int* counters_ = nullptr;
+  int* active_host_ = nullptr;
+  int rpt_[kClasses] = {};
+  float tune_ms_[kClasses][3] = {};
+  cudaGraph_t graph_ = nullptr;
+  cudaGraphExec_t graph_exec_ = nullptr;
+  unsigned int graph_sig_ = 0;
+  long long graph_kernels_ = 0;
+};
+
+}  // namespace mgb
