@@ -43,6 +43,12 @@ sys.path.insert(0, str(ROOT))
 METRIC = "kernel-CG solves/s & p99 latency at relres 1e-10: mixed vs plain FP64, 1 GB300"
 N_FULL, DIM, ELL, NUGGET, EPS = 65536, 2, 0.05, 1e-4, 1e-10
 L2_FLUSH_BYTES = 512 << 20
+# FP64 CG iterations of the full n = 65536 solve, measured once on GB300 with
+# mgb_cg_gauss (plain FP64, 1163.6 s); used to turn sampled FP64 and
+# reference iterations into solves/s.  Other sizes fall back to the mixed
+# count (a lower bound on the FP64 count for this family).
+FP64_ITERATIONS_N65536 = 18958
+SFU_EX2_PER_CLK_SM = 32.0
 SMI_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -130,6 +136,19 @@ def aggregate(units_per_rank: float, seconds_max: float, world: int) -> float:
 
 
 # -------------------------------------------------------------- CPU baseline
+def measured_peak(key: str):
+    try:
+        return float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())[key])
+    except (OSError, KeyError, ValueError, TypeError):
+        return None
+
+
+def fp64_iterations(args, fallback: int) -> int:
+    if args.fp64_iterations:
+        return args.fp64_iterations
+    return FP64_ITERATIONS_N65536 if args.n == N_FULL else fallback
+
+
 def cpu_baseline(points_scaled: np.ndarray, nugget: float, iterations: int, budget_s: float = 10.0) -> dict:
     """FP64 oracle matvec rows on the host cores for about budget_s seconds;
     solves/s = entries/s / (n^2 * iterations)."""
@@ -154,6 +173,133 @@ def cpu_baseline(points_scaled: np.ndarray, nugget: float, iterations: int, budg
             "sample": f"{done_entries / 1e9:.2f}e9 FP64 kernel entries of the C oracle matvec ({dt:.1f} s, "
                       f"OpenMP over rows), scaled by n^2 x {iterations} CG iterations per solve",
             "entries_per_s": eps}
+
+
+# ------------------------------------------------------- secondary sections
+def bench_dense(mg, torch, stream, hbm_peak_gbs: float | None) -> dict:
+    """Dense FP64 CG (n = 4096, A = M^T M / n + I, b = 1, relres 1e-10) and
+    the dgemv on the same A."""
+    from mpla_gb300 import synth
+
+    n = 4096
+    A, b, _ = synth.config_dense(0)
+    dA = mg.DeviceArray.from_numpy(np.asfortranarray(A).ravel(order="F"))
+    db = mg.DeviceArray.from_numpy(b)
+    dy = mg.DeviceArray(n)
+    x_t = torch.zeros(n, dtype=torch.float64, device="cuda")  # zeroed in order on the bench stream
+    torch.cuda.synchronize()
+    sp = stream.cuda_stream
+    reps = 20
+
+    def solve():
+        with torch.cuda.stream(stream):
+            x_t.zero_()
+            return mg.cg_dense(n, dA.ptr, db.ptr, x_t.data_ptr(), iter_max=1000, eps=EPS, stream=sp)
+
+    for _ in range(3):
+        info = solve()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        info = solve()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    solve_ms = e0.elapsed_time(e1) / reps
+    gemv_ms = mg.time_dgemv(n, dA.ptr, db.ptr, dy.ptr, reps=50, stream=sp)
+    gemv_bytes = 8.0 * n * n + 16.0 * n
+    gbs = gemv_bytes / (gemv_ms * 1e-3) / 1e9
+    return {"workload": "dense FP64 CG, n=4096, A = M^T M/n + I (M ~ U[-1,1], seed 0), b = 1, relres 1e-10",
+            "solves_per_s": 1e3 / solve_ms, "ms_per_solve": solve_ms, "iterations": int(info.iterations),
+            "converged": int(info.status) == 0,
+            "dgemv": {"ms": gemv_ms, "achieved_gbs": gbs, "peak_gbs": hbm_peak_gbs,
+                      "frac": gbs / hbm_peak_gbs if hbm_peak_gbs else None,
+                      "bytes": gemv_bytes, "note": "A is 128 MiB: back-to-back launches partly hit L2"}}
+
+
+def bench_batched(mg, count: int, check_rows: int = 4096) -> dict:
+    """Batched mixed-precision solves: `count` Gaussian systems (n log-uniform
+    in [256, 16384], d in {2,3}, l ~ U[0.03, 0.2], nugget 1e-4, 1-8 N(0,1)
+    right-hand sides), admitted together and run to relres 1e-10."""
+    import oracle
+    from mpla_gb300 import synth
+
+    spec = synth.batch_spec(count)
+    systems = [synth.batch_system(spec, k) for k in range(count)]
+    batch = mg.Batch(count)
+    t_add0 = time.perf_counter()
+    handles = []
+    for g in systems:
+        handles.append(batch.add(g.scaled(), g.nugget, g.b, precision=mg.PREC_MIXED, eps=EPS, iter_max=300000))
+    mg.synchronize()
+    t_add = time.perf_counter() - t_add0
+    launches0 = mg.kernel_launches()
+    t0 = time.perf_counter()
+    left = batch.run()
+    mg.synchronize()
+    sec = time.perf_counter() - t0
+    launches = mg.kernel_launches() - launches0
+    iters, statuses, worst_oracle = [], [], 0.0
+    rhs_total = 0
+    for k, (h, g) in enumerate(zip(handles, systems)):
+        x, infos = batch.result(h, g.n, g.b.shape[1])
+        rhs_total += g.b.shape[1]
+        iters += [i.iterations for i in infos]
+        statuses += [int(i.status) for i in infos]
+        if g.n <= check_rows and k % 16 == 0:   # oracle check on a sample of the smaller systems
+            op = oracle.GaussOp(g.scaled(), g.nugget)
+            worst_oracle = max(worst_oracle, max(oracle.true_relres(op, g.b[:, j], x[:, j])
+                                                 for j in range(g.b.shape[1])))
+    rpt, _ = batch.tuning()
+    batch.close()
+    return {"workload": f"{count} Gaussian systems, n log-uniform [256,16384], d in {{2,3}}, l ~ U[0.03,0.2], "
+                        "nugget 1e-4, 1-8 N(0,1) right-hand sides, mixed precision, relres 1e-10",
+            "systems_per_s": count / sec, "rhs_solves_per_s": rhs_total / sec, "seconds": sec,
+            "e2e_systems_per_s": count / (sec + t_add), "admission_seconds": t_add,
+            "unfinished": left, "all_converged": all(s == 0 for s in statuses),
+            "iterations_median": float(np.median(iters)), "iterations_max": int(max(iters)),
+            "oracle_worst_relres_sampled": worst_oracle, "gpu_launches": int(launches),
+            "autotuner_rows_per_thread": rpt}
+
+
+def bench_serving(mg, rate: float, window: float, drain: float, seed: int = 0) -> dict:
+    """Continuous batching: Poisson arrivals at `rate` per second for `window`
+    seconds; n log-uniform in [1024, 32768], d in {2,3}, l ~ U[0.03, 0.2],
+    1-4 N(0,1) right-hand sides, half FP64 and half mixed, relres 1e-10."""
+    from mpla_gb300 import synth
+    from mpla_gb300.serve import Request, Server, latency_stats, poisson_arrivals
+
+    rng = np.random.default_rng(seed)
+    arrivals = poisson_arrivals(rate, window, rng)
+    reqs = []
+    for k, a in enumerate(arrivals):
+        n = int(np.exp(rng.uniform(np.log(1024), np.log(32768))))
+        dim = 2 + int(rng.random() < 0.5)
+        ell = float(rng.uniform(0.03, 0.2))
+        r = int(rng.integers(1, 5))
+        pts = np.stack([synth.uniform(seed, 5000 + 16 * k + j, n) for j in range(dim)]) / (math.sqrt(2.0) * ell)
+        b = np.stack([synth.normal(seed, 6_000_000 + 16 * k + j, n) for j in range(r)], axis=1)
+        reqs.append((a, k, pts, b))
+    batch = mg.Batch(256)
+    srv = Server(batch, slice_steps=64)
+    t0 = time.perf_counter()
+    for a, k, pts, b in reqs:
+        srv.submit(Request(arrival=t0 + a, rid=k, points=pts, b=b, precision=k % 2))
+    srv.serve(until=t0 + window, drain_until=t0 + window + drain)
+    st = latency_stats(srv.done)
+    conv = all(int(i.status) == 0 for c in srv.done for i in c.infos)
+    by_prec = {}
+    for p, name in ((0, "fp64"), (1, "mixed")):
+        lat = [c.latency for c in srv.done if c.precision == p]
+        if lat:
+            by_prec[name] = {"completed": len(lat), "p50_s": float(np.percentile(lat, 50)),
+                             "p99_s": float(np.percentile(lat, 99))}
+    batch.close()
+    st.update({"workload": f"Poisson arrivals {rate}/s for {window} s, n log-uniform [1024,32768], d in {{2,3}}, "
+                           "l ~ U[0.03,0.2], 1-4 N(0,1) right-hand sides, half FP64 / half mixed, relres 1e-10",
+               "submitted": len(reqs), "unfinished": len(reqs) - len(srv.done), "all_converged": conv,
+               "admission_refusals": srv.refusals, "by_precision": by_prec})
+    return st
 
 
 # ---------------------------------------------------------------- our arm
@@ -262,17 +408,22 @@ def run_ours(args, world, rank, local):
     sm_mhz = clocks.get("sm_mhz") or 1900.0
     entries = float(n) * n
     mixed_rate = entries / (mixed_ms * 1e-3)
-    sfu_peak = 16.0 * sms * sm_mhz * 1e6
+    sfu_peak = SFU_EX2_PER_CLK_SM * sms * sm_mhz * 1e6
     fp64_rate = entries / (f64_ms * 1e-3)
 
     iters_mixed = int(info.iterations)
-    # FP64 CG iteration count for this system: measured once with a full
-    # FP64 solve (see profiles/); until then the mixed count stands in.
-    iters_fp64 = args.fp64_iterations or iters_mixed
+    iters_fp64 = fp64_iterations(args, iters_mixed)
     fp64_solves_est = 1.0 / (fp_ms_per_iter * 1e-3 * iters_fp64)
 
     if rank != 0:
         return
+    extra = {}
+    if not args.no_dense:
+        extra["dense"] = bench_dense(mg, torch, stream, measured_peak("hbm_gbs"))
+    if not args.no_batched:
+        extra["batched"] = bench_batched(mg, args.batch_systems)
+    if not args.no_serving:
+        extra["serving"] = bench_serving(mg, args.serve_rate, args.serve_window, args.serve_drain)
     cpu = cpu_baseline(pts_scaled, NUGGET, iters_fp64, budget_s=args.cpu_seconds) if not args.no_cpu else None
     line = {
         "metric": METRIC,
@@ -308,11 +459,13 @@ def run_ours(args, world, rank, local):
                      "achieved": mixed_rate / 1e12, "peak": sfu_peak / 1e12, "unit": "Tex2/s",
                      "frac": mixed_rate / sfu_peak, "traffic": None,
                      "per_unit": "1 kernel entry = 1 ex2 + 6 FP32 ops; n^2 entries per launch",
-                     "peak_source": f"nominal 16 ex2/clk/SM x {sms} SMs x {sm_mhz:.0f} MHz median SM clock"},
+                     "peak_source": f"{SFU_EX2_PER_CLK_SM:.0f} ex2/clk/SM (the XU pipe peak ncu reports on GB300) "
+                                    f"x {sms} SMs x {sm_mhz:.0f} MHz median SM clock"},
         "cpu_baseline": cpu,
         "gpu_launches": int(launches),
         "clocks": clocks,
     }
+    line.update(extra)
     print(json.dumps(line), flush=True)
 
 
@@ -363,7 +516,7 @@ def run_reference(args, world, rank, local):
         total_ms += ms.value
         total_it += it.value
     ms_per_iter = total_ms / max(1, total_it)
-    iters_fp64 = args.fp64_iterations or 0
+    iters_fp64 = fp64_iterations(args, 0)
     value = (1.0 / (ms_per_iter * 1e-3 * iters_fp64)) if iters_fp64 else None
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": 1,
@@ -398,6 +551,13 @@ def main(argv=None):
     p.add_argument("--ref-sample-iters", type=int, default=3)
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-dense", action="store_true")
+    p.add_argument("--no-batched", action="store_true")
+    p.add_argument("--no-serving", action="store_true")
+    p.add_argument("--batch-systems", type=int, default=512)
+    p.add_argument("--serve-rate", type=float, default=2.0)
+    p.add_argument("--serve-window", type=float, default=10.0)
+    p.add_argument("--serve-drain", type=float, default=120.0)
     args = p.parse_args(argv)
     if args.warmup < 3:
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

@@ -149,8 +149,10 @@ __global__ void __launch_bounds__(T) k_rr(int n, const double* __restrict__ r, S
 // (skipped unless a replacement is due); k_mx_replace; direction.
 // Replacement (reliable update) when the recursive residual has dropped by
 // `delta` since the last true residual, when it claims convergence, or at
-// the iteration cap.  Convergence is only ever declared on the FP64 true
-// residual ||b - A_hi x|| / ||b||.
+// the iteration cap; the search direction then restarts from the true
+// residual (iterative refinement with a CG inner solve that keeps x).
+// Convergence is only ever declared on the FP64 true residual
+// ||b - A_hi x|| / ||b||.
 __global__ void __launch_bounds__(T) k_mx_update(int n, const double* __restrict__ d, const double* __restrict__ z,
                                                  double* __restrict__ x, double* __restrict__ r, SolverState* st,
                                                  double delta2, RedCtx rc) {
@@ -198,7 +200,9 @@ __global__ void __launch_bounds__(T) k_mx_replace(int n, const double* __restric
     st->res = res;
     if (hist) hist[st->k] = res;
     *replacements += 1;
-    st->beta = rr_true / st->rr;
+    // restart the direction from the true residual: the FP32 operator's
+    // perturbation leaves the old direction's conjugacy unusable once r jumps
+    st->beta = 0.0;
     st->rr = rr_true;
     st->rr_ref = rr_true;
     st->flag = 1;
