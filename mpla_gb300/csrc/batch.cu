@@ -17,8 +17,9 @@
 //   update  one CTA per system: x += alpha d, r -= alpha z, new <r,r>; mixed
 //           lanes decide whether the FP64 true residual is due
 //   mv64r   persistent kernel over items of mixed systems with a pending
-//           replacement: z = K x in FP64 (returns at once otherwise)
-//   replace one CTA per system: r = b - z for those lanes, convergence test
+//           replacement: z = b - K x in double-double (returns at once
+//           otherwise)
+//   replace one CTA per system: r = z for those lanes, convergence test
 //           on the FP64 true residual, restart of the direction
 //   dir     one CTA per system: d = beta d + r (and its FP32 copy)
 // Systems and item lists live in device memory, so systems are added and
@@ -35,7 +36,7 @@
 // direction's conjugacy unusable once r jumps).  Convergence is declared only
 // on the FP64 true residual.
 //
-// Rows per thread of the FP32 matvec (1, 2 or 4) are chosen per (dim, R)
+// Rows per thread of the FP32 matvec (2 or 4) are chosen per (dim, R)
 // class by timing each variant on the class's items at first use.
 #include <algorithm>
 #include <cmath>
@@ -95,12 +96,51 @@ __device__ __forceinline__ void queue_done(const WorkQueue& q) {
 }
 
 // ------------------------------------------------------- FP32 matvec
-// z = K~ d + nugget d for the R lanes of mixed systems of one class.
+// Packed FP32 pairs (Blackwell f32x2 instructions): one instruction applies
+// the same operation to two rows.
+__device__ __forceinline__ uint64_t f2_pack(float lo, float hi) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void f2_unpack(uint64_t v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ uint64_t f2_add(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ uint64_t f2_sub(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ uint64_t f2_mul(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
+  uint64_t r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+
+// z = K~ d + nugget d for the R lanes of mixed systems of one class.  A
+// thread owns RPT rows (RPT/2 packed pairs: rows r and r + 128 of a pair of
+// tiles); column values are staged in shared memory twice over so that one
+// load gives a packed operand.  Coordinate differences are
+// fl(fl(hi_i - hi_j) + fl(lo_i - lo_j)): exact-symmetric and accurate to the
+// rounding of the difference itself.  Per 128-column tile the products are
+// summed in FP32, and the tile sums in FP64.
 template <int DIM, int R, int RPT>
 __global__ void __launch_bounds__(kTile) k_bmv32(WorkQueue q, const BatchSys* __restrict__ sys) {
-  __shared__ float4 sh[kColTile];
-  __shared__ float4 sl[kColTile];
-  __shared__ float sd[kColTile * R];
+  constexpr int NP = RPT / 2;  // packed row pairs per thread
+  __shared__ float4 shx[kColTile];  // {hx, hx, hy, hy}
+  __shared__ float4 slx[kColTile];  // {lx, lx, ly, ly}
+  __shared__ float4 sz[kColTile];   // {hz, hz, lz, lz}
+  __shared__ float2 sd[kColTile * R];
   __shared__ int s_item;
   for (;;) {
     const int it = claim(q, &s_item);
@@ -112,13 +152,20 @@ __global__ void __launch_bounds__(kTile) k_bmv32(WorkQueue q, const BatchSys* __
     // RPT consecutive tiles and takes only every RPT-th item
     if ((w.row0 / kTile) % RPT != 0) continue;
     const int n = S.n;
-    float4 hi[RPT], lo[RPT];
+    uint64_t hx[NP], hy[NP], hz[NP], lx[NP], ly[NP], lz[NP];
     int row[RPT];
 #pragma unroll
-    for (int a = 0; a < RPT; ++a) {
-      row[a] = w.row0 + threadIdx.x + kTile * a;
-      hi[a] = S.pts_hi[min(row[a], n - 1)];
-      lo[a] = S.pts_lo[min(row[a], n - 1)];
+    for (int p = 0; p < NP; ++p) {
+      row[2 * p] = w.row0 + threadIdx.x + kTile * (2 * p);
+      row[2 * p + 1] = row[2 * p] + kTile;
+      const float4 h0 = S.pts_hi[min(row[2 * p], n - 1)], h1 = S.pts_hi[min(row[2 * p + 1], n - 1)];
+      const float4 l0 = S.pts_lo[min(row[2 * p], n - 1)], l1 = S.pts_lo[min(row[2 * p + 1], n - 1)];
+      hx[p] = f2_pack(h0.x, h1.x);
+      hy[p] = f2_pack(h0.y, h1.y);
+      hz[p] = f2_pack(h0.z, h1.z);
+      lx[p] = f2_pack(l0.x, l1.x);
+      ly[p] = f2_pack(l0.y, l1.y);
+      lz[p] = f2_pack(l0.z, l1.z);
     }
     double acc[RPT][R];
 #pragma unroll
@@ -130,44 +177,67 @@ __global__ void __launch_bounds__(kTile) k_bmv32(WorkQueue q, const BatchSys* __
       __syncthreads();
       for (int t = threadIdx.x; t < kColTile; t += kTile) {
         const bool in = t < nj;
-        sh[t] = in ? S.pts_hi[j0 + t] : make_float4(0.f, 0.f, 0.f, 0.f);
-        sl[t] = in ? S.pts_lo[j0 + t] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 h = in ? S.pts_hi[j0 + t] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 l = in ? S.pts_lo[j0 + t] : make_float4(0.f, 0.f, 0.f, 0.f);
+        shx[t] = make_float4(h.x, h.x, h.y, h.y);
+        slx[t] = make_float4(l.x, l.x, l.y, l.y);
+        sz[t] = make_float4(h.z, h.z, l.z, l.z);
 #pragma unroll
-        for (int k = 0; k < R; ++k) sd[t * R + k] = in ? S.d32[(long long)(j0 + t) * R + k] : 0.f;
+        for (int k = 0; k < R; ++k) {
+          const float v = in ? S.d32[(long long)(j0 + t) * R + k] : 0.f;
+          sd[t * R + k] = make_float2(v, v);
+        }
       }
       __syncthreads();
-      float part[RPT][R];
+      uint64_t part[NP][R];
 #pragma unroll
-      for (int a = 0; a < RPT; ++a)
+      for (int p = 0; p < NP; ++p)
 #pragma unroll
-        for (int k = 0; k < R; ++k) part[a][k] = 0.f;
+        for (int k = 0; k < R; ++k) part[p][k] = 0ull;
 #pragma unroll 2
       for (int t = 0; t < nj; ++t) {
-        const float4 ph = sh[t];
-        const float4 pl = sl[t];
-        float dv[R];
+        const float4 H = shx[t], L = slx[t];
+        const uint64_t qhx = f2_pack(H.x, H.y), qhy = f2_pack(H.z, H.w);
+        const uint64_t qlx = f2_pack(L.x, L.y), qly = f2_pack(L.z, L.w);
+        uint64_t qhz = 0ull, qlz = 0ull;
+        if (DIM == 3) {
+          const float4 Z = sz[t];
+          qhz = f2_pack(Z.x, Z.y);
+          qlz = f2_pack(Z.z, Z.w);
+        }
+        uint64_t dv[R];
 #pragma unroll
-        for (int k = 0; k < R; ++k) dv[k] = sd[t * R + k];
+        for (int k = 0; k < R; ++k) {
+          const float2 v = sd[t * R + k];
+          dv[k] = f2_pack(v.x, v.y);
+        }
 #pragma unroll
-        for (int a = 0; a < RPT; ++a) {
-          const float dx = (hi[a].x - ph.x) + (lo[a].x - pl.x);
-          const float dy = (hi[a].y - ph.y) + (lo[a].y - pl.y);
-          float ns;
+        for (int p = 0; p < NP; ++p) {
+          const uint64_t dx = f2_add(f2_sub(hx[p], qhx), f2_sub(lx[p], qlx));
+          const uint64_t dy = f2_add(f2_sub(hy[p], qhy), f2_sub(ly[p], qly));
+          uint64_t s2;
           if (DIM == 2) {
-            ns = fmaf(-dx, dx, -dy * dy);
+            s2 = f2_fma(dx, dx, f2_mul(dy, dy));
           } else {
-            const float dz = (hi[a].z - ph.z) + (lo[a].z - pl.z);
-            ns = fmaf(-dx, dx, fmaf(-dy, dy, -dz * dz));
+            const uint64_t dz = f2_add(f2_sub(hz[p], qhz), f2_sub(lz[p], qlz));
+            s2 = f2_fma(dx, dx, f2_fma(dy, dy, f2_mul(dz, dz)));
           }
-          const float e = ex2_approx(ns);
+          float s0, s1;
+          f2_unpack(s2, s0, s1);
+          const uint64_t e2 = f2_pack(ex2_approx(-s0), ex2_approx(-s1));
 #pragma unroll
-          for (int k = 0; k < R; ++k) part[a][k] = fmaf(e, dv[k], part[a][k]);
+          for (int k = 0; k < R; ++k) part[p][k] = f2_fma(e2, dv[k], part[p][k]);
         }
       }
 #pragma unroll
-      for (int a = 0; a < RPT; ++a)
+      for (int p = 0; p < NP; ++p)
 #pragma unroll
-        for (int k = 0; k < R; ++k) acc[a][k] += (double)part[a][k];
+        for (int k = 0; k < R; ++k) {
+          float a0, a1;
+          f2_unpack(part[p][k], a0, a1);
+          acc[2 * p][k] += (double)a0;
+          acc[2 * p + 1][k] += (double)a1;
+        }
     }
 #pragma unroll
     for (int a = 0; a < RPT; ++a) {
@@ -184,10 +254,24 @@ __global__ void __launch_bounds__(kTile) k_bmv32(WorkQueue q, const BatchSys* __
 }
 
 // ------------------------------------------------------- FP64 matvec
-// mode Q_MV64: z = K d for FP64 systems; mode Q_MV64_TRUE: z = K x for mixed
-// systems with a pending true-residual replacement.
-template <int DIM, int R>
-__global__ void __launch_bounds__(kTile) k_bmv64(WorkQueue q, const BatchSys* __restrict__ sys, int mode,
+// TRUE_RES = false: z = K d + nugget d for FP64 systems (the reference's
+// FP64 iteration).  TRUE_RES = true: z = b - (K x + nugget x), the true
+// residual of mixed systems with a pending replacement, with every row's sum
+// kept in double-double (products split exactly by fma, sums by TwoSum: the
+// compensated dot product of Ogita, Rump and Oishi).  On these systems x
+// reaches ~1e4 ||b|| and a plain FP64 sum of K_ij x_j carries noise of about
+// u * sum_j |K_ij x_j|, i.e. ~1e-10 relative: the very tolerance the mixed
+// iteration must certify.
+__device__ __forceinline__ void dd_add(double& s, double& c, double p, double pe) {
+  const double t = __dadd_rn(s, p);
+  const double bp = __dsub_rn(t, s);
+  const double e = __dadd_rn(__dsub_rn(s, __dsub_rn(t, bp)), __dsub_rn(p, bp));
+  s = t;
+  c = __dadd_rn(c, __dadd_rn(e, pe));
+}
+
+template <int DIM, int R, bool TRUE_RES>
+__global__ void __launch_bounds__(kTile) k_bmv64(WorkQueue q, const BatchSys* __restrict__ sys,
                                                  const double* __restrict__ table_g) {
   __shared__ double table[kExpTableSize];
   __shared__ double sp[DIM][kColTile];
@@ -200,17 +284,17 @@ __global__ void __launch_bounds__(kTile) k_bmv64(WorkQueue q, const BatchSys* __
     const BatchItem w = q.items[it];
     const BatchSys& S = sys[w.sys];
     if (!sys_active(S) || S.dim != DIM || S.R != R) continue;
-    if (mode == Q_MV64 && S.precision != MGB_PREC_FP64) continue;
-    if (mode == Q_MV64_TRUE && (S.precision != MGB_PREC_MIXED || !S.need_hi)) continue;
+    if (!TRUE_RES && S.precision != MGB_PREC_FP64) continue;
+    if (TRUE_RES && (S.precision != MGB_PREC_MIXED || !S.need_hi)) continue;
     const int n = S.n;
-    const double* v = mode == Q_MV64 ? S.d : S.x;
+    const double* v = TRUE_RES ? S.x : S.d;
     const int i = w.row0 + threadIdx.x;
     double pi[DIM];
 #pragma unroll
     for (int d = 0; d < DIM; ++d) pi[d] = S.pts64[(long long)d * n + min(i, n - 1)];
-    double acc[R];
+    double acc[R], cmp[R];
 #pragma unroll
-    for (int k = 0; k < R; ++k) acc[k] = 0.0;
+    for (int k = 0; k < R; ++k) acc[k] = cmp[k] = 0.0;
     for (int j0 = 0; j0 < n; j0 += kColTile) {
       const int nj = min(kColTile, n - j0);
       __syncthreads();
@@ -231,14 +315,30 @@ __global__ void __launch_bounds__(kTile) k_bmv64(WorkQueue q, const BatchSys* __
         }
         const double e = exp_neg_table(s, table);
 #pragma unroll
-        for (int k = 0; k < R; ++k) acc[k] = fma(e, sv[t * R + k], acc[k]);
+        for (int k = 0; k < R; ++k) {
+          const double vk = sv[t * R + k];
+          if (TRUE_RES) {
+            const double p = __dmul_rn(e, vk);
+            dd_add(acc[k], cmp[k], p, fma(e, vk, -p));
+          } else {
+            acc[k] = fma(e, vk, acc[k]);
+          }
+        }
       }
     }
     if (i < n) {
 #pragma unroll
       for (int k = 0; k < R; ++k) {
         const long long o = (long long)i * R + k;
-        S.z[o] = fma(S.nugget, v[o], acc[k]);
+        if (TRUE_RES) {
+          const double p = __dmul_rn(S.nugget, v[o]);
+          dd_add(acc[k], cmp[k], p, fma(S.nugget, v[o], -p));
+          // b - (acc + cmp): b and acc agree to a few digits, so b - acc is
+          // exact or nearly so
+          S.z[o] = __dsub_rn(__dsub_rn(S.b[o], acc[k]), cmp[k]);
+        } else {
+          S.z[o] = fma(S.nugget, v[o], acc[k]);
+        }
       }
     }
   }
@@ -361,7 +461,7 @@ __device__ void vec_replace(BatchSys& S, double* smem) {
     for (int k = 0; k < R; ++k) {
       if (!s_flag[k]) continue;
       const long long o = (long long)i * R + k;
-      const double ri = S.b[o] - S.z[o];
+      const double ri = S.z[o];  // b - K x from the double-double matvec
       S.r[o] = ri;
       v[k] = fma(ri, ri, v[k]);
     }
@@ -677,8 +777,7 @@ static WorkQueue make_queue(const BatchItem* items, int* counters, int cls, int 
 template <int DIM, int R>
 static void launch_mv32(const WorkQueue& q, const BatchSys* sys, int rpt, int grid, cudaStream_t s) {
   if (rpt == 4) k_bmv32<DIM, R, 4><<<grid, kTile, 0, s>>>(q, sys);
-  else if (rpt == 2) k_bmv32<DIM, R, 2><<<grid, kTile, 0, s>>>(q, sys);
-  else k_bmv32<DIM, R, 1><<<grid, kTile, 0, s>>>(q, sys);
+  else k_bmv32<DIM, R, 2><<<grid, kTile, 0, s>>>(q, sys);
 }
 
 int BatchEngine::enqueue_mv32(int cls, int rpt) {
@@ -699,19 +798,27 @@ int BatchEngine::enqueue_mv32(int cls, int rpt) {
   return MGB_OK;
 }
 
+template <int DIM, int R>
+static void launch_mv64(const WorkQueue& q, const BatchSys* sys, bool true_res, const double* table, int grid,
+                        cudaStream_t s) {
+  if (true_res) k_bmv64<DIM, R, true><<<grid, kTile, 0, s>>>(q, sys, table);
+  else k_bmv64<DIM, R, false><<<grid, kTile, 0, s>>>(q, sys, table);
+}
+
 int BatchEngine::enqueue_mv64(int cls, int mode) {
   const WorkQueue q = make_queue(items_[cls], counters_, cls, mode, kClasses);
   const int grid = 2 * c_->num_sms;
   const double* t = c_->exp_table;
+  const bool tr = mode == Q_MV64_TRUE;
   switch (cls) {
-    case 0: k_bmv64<2, 1><<<grid, kTile, 0, s_>>>(q, dev_sys_, mode, t); break;
-    case 1: k_bmv64<2, 2><<<grid, kTile, 0, s_>>>(q, dev_sys_, mode, t); break;
-    case 2: k_bmv64<2, 4><<<grid, kTile, 0, s_>>>(q, dev_sys_, mode, t); break;
-    case 3: k_bmv64<2, 8><<<grid, kTile, 0, s_>>>(q, dev_sys_, mode, t); break;
-    case 4: k_bmv64<3, 1><<<grid, kTile, 0, s_>>>(q, dev_sys_, mode, t); break;
-    case 5: k_bmv64<3, 2><<<grid, kTile, 0, s_>>>(q, dev_sys_, mode, t); break;
-    case 6: k_bmv64<3, 4><<<grid, kTile, 0, s_>>>(q, dev_sys_, mode, t); break;
-    default: k_bmv64<3, 8><<<grid, kTile, 0, s_>>>(q, dev_sys_, mode, t); break;
+    case 0: launch_mv64<2, 1>(q, dev_sys_, tr, t, grid, s_); break;
+    case 1: launch_mv64<2, 2>(q, dev_sys_, tr, t, grid, s_); break;
+    case 2: launch_mv64<2, 4>(q, dev_sys_, tr, t, grid, s_); break;
+    case 3: launch_mv64<2, 8>(q, dev_sys_, tr, t, grid, s_); break;
+    case 4: launch_mv64<3, 1>(q, dev_sys_, tr, t, grid, s_); break;
+    case 5: launch_mv64<3, 2>(q, dev_sys_, tr, t, grid, s_); break;
+    case 6: launch_mv64<3, 4>(q, dev_sys_, tr, t, grid, s_); break;
+    default: launch_mv64<3, 8>(q, dev_sys_, tr, t, grid, s_); break;
   }
   count_launches(1);
   MGB_CUDA(cudaGetLastError());
@@ -722,7 +829,7 @@ int BatchEngine::enqueue_step() {
   const double delta2 = 1e-4;  // replacement when the recursive residual fell 100x
   for (int cls = 0; cls < kClasses; ++cls) {
     if (!count_host_[cls]) continue;
-    MGB_TRY(enqueue_mv32(cls, rpt_[cls] ? rpt_[cls] : 1));
+    MGB_TRY(enqueue_mv32(cls, rpt_[cls] ? rpt_[cls] : 2));
     MGB_TRY(enqueue_mv64(cls, Q_MV64));
   }
   k_bvec<0><<<nslots_, kVecThreads, 0, s_>>>(dev_sys_, nslots_, delta2);
@@ -752,8 +859,8 @@ int BatchEngine::autotune() {
     for (const BatchItem& w : items_host_[cls]) mixed |= host_[w.sys].precision == MGB_PREC_MIXED;
     if (!mixed) continue;
     float best = 1e30f;
-    int best_rpt = 1;
-    for (int v = 0; v < 3 && st == MGB_OK; ++v) {
+    int best_rpt = 2;
+    for (int v = 1; v < 3 && st == MGB_OK; ++v) {
       const int rpt = 1 << v;
       st = enqueue_mv32(cls, rpt);  // warm-up
       if (st != MGB_OK) break;

@@ -220,6 +220,40 @@ __device__ __forceinline__ void warp_reduce_scatter32(float (&v)[32], int lane) 
   }
 }
 
+// Packed FP32 pairs (Blackwell f32x2 instructions): one instruction applies
+// the same operation to two rows.
+__device__ __forceinline__ uint64_t f2_pack(float lo, float hi) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void f2_unpack(uint64_t v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ uint64_t f2_sub(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ uint64_t f2_mul(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
+  uint64_t r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+
+// Per column t of tile J the shared arrays hold each value twice, so that one
+// 128-bit load gives packed operands: cq[t] = {x, x, y, y},
+// cw[t] = {z, z, x_t, x_t} (x_t the FP32 vector entry).  Lane l's rows pair
+// up as (l, l+32) and (l+64, l+96).  Per pair of entries: two packed
+// subtractions (three for d = 3), a packed multiply and FMA for the squared
+// distance, two MUFU.EX2, a packed FMA into the row sums and one into the
+// column partial -- the same arithmetic, entry for entry, as the scalar form
+// fl(fl(dx^2 + fl(dy^2))) with dx = fl(x_i - x_j).
 template <int DIM>
 __global__ void __launch_bounds__(kF32Threads) sym_f32_pair_kernel(int n, int T, const float4* __restrict__ pts,
                                                                    const double* __restrict__ centers,
@@ -227,58 +261,78 @@ __global__ void __launch_bounds__(kF32Threads) sym_f32_pair_kernel(int n, int T,
                                                                    float* __restrict__ S,
                                                                    const int* __restrict__ skip) {
   if (skip && *skip) return;
-  __shared__ float4 sp[2][kB];
+  __shared__ float4 sr[kB];
+  __shared__ float4 cq[kB];
+  __shared__ float4 cw[kB];
   __shared__ float rowbuf[4][kB];
   __shared__ float s_dc[3];
   int I, J;
   cta_pair(T, &I, &J);
+  if (threadIdx.x < 3) s_dc[threadIdx.x] = (float)(centers[3 * I + threadIdx.x] - centers[3 * J + threadIdx.x]);
   for (int t = threadIdx.x; t < 2 * kB; t += kF32Threads) {
     const int side = t / kB, k = t % kB;
     const int g = (side ? J : I) * kB + k;
     float4 p = pts[g];  // padded to whole tiles
     p.w = (g < n) ? xf[g] : 0.f;
-    sp[side][k] = p;
+    if (side == 0) {
+      sr[k] = p;
+    } else {
+      cq[k] = make_float4(p.x, p.x, p.y, p.y);
+      cw[k] = make_float4(p.z, p.z, p.w, p.w);
+    }
   }
-  if (threadIdx.x < 3) s_dc[threadIdx.x] = (float)(centers[3 * I + threadIdx.x] - centers[3 * J + threadIdx.x]);
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  float ri[4][DIM], xi[4];
+  uint64_t rx[2], ry[2], rz[2], xi2[2], acc[2];
 #pragma unroll
-  for (int a = 0; a < 4; ++a) {
-    const float4 p = sp[0][lane + 32 * a];
-    ri[a][0] = p.x + s_dc[0];
-    if (DIM > 1) ri[a][1 % DIM] = p.y + s_dc[1];
-    if (DIM > 2) ri[a][2 % DIM] = p.z + s_dc[2];
-    xi[a] = p.w;
+  for (int q = 0; q < 2; ++q) {
+    const float4 a = sr[lane + 64 * q];
+    const float4 b = sr[lane + 64 * q + 32];
+    rx[q] = f2_pack(a.x + s_dc[0], b.x + s_dc[0]);
+    ry[q] = f2_pack(a.y + s_dc[1], b.y + s_dc[1]);
+    rz[q] = f2_pack(a.z + s_dc[2], b.z + s_dc[2]);
+    xi2[q] = f2_pack(a.w, b.w);
+    acc[q] = 0ull;  // +0.0f in both halves
   }
-  float acc_r[4] = {0.f, 0.f, 0.f, 0.f};
   float col[32];
 #pragma unroll
   for (int b = 0; b < 32; ++b) {
-    const float4 q = sp[1][32 * warp + b];
-    float c = 0.f;
+    const float4 q4 = cq[32 * warp + b];
+    const float4 w4 = cw[32 * warp + b];
+    const uint64_t qx = f2_pack(q4.x, q4.y), qy = f2_pack(q4.z, q4.w);
+    const uint64_t qz = f2_pack(w4.x, w4.y), qw = f2_pack(w4.z, w4.w);
+    uint64_t c2 = 0ull;
 #pragma unroll
-    for (int a = 0; a < 4; ++a) {
-      const float dx = ri[a][0] - q.x;
-      float ns;
+    for (int q = 0; q < 2; ++q) {
+      const uint64_t dx = f2_sub(rx[q], qx);
+      uint64_t s2;
       if (DIM == 1) {
-        ns = -dx * dx;
+        s2 = f2_mul(dx, dx);
       } else if (DIM == 2) {
-        const float dy = ri[a][1 % DIM] - q.y;
-        ns = fmaf(-dx, dx, -dy * dy);
+        const uint64_t dy = f2_sub(ry[q], qy);
+        s2 = f2_fma(dx, dx, f2_mul(dy, dy));
       } else {
-        const float dy = ri[a][1 % DIM] - q.y;
-        const float dz = ri[a][2 % DIM] - q.z;
-        ns = fmaf(-dx, dx, fmaf(-dy, dy, -dz * dz));
+        const uint64_t dy = f2_sub(ry[q], qy);
+        const uint64_t dz = f2_sub(rz[q], qz);
+        s2 = f2_fma(dx, dx, f2_fma(dy, dy, f2_mul(dz, dz)));
       }
-      const float e = ex2_approx(ns);
-      acc_r[a] = fmaf(e, q.w, acc_r[a]);
-      c = fmaf(e, xi[a], c);
+      float s0, s1;
+      f2_unpack(s2, s0, s1);
+      const uint64_t e2 = f2_pack(ex2_approx(-s0), ex2_approx(-s1));
+      acc[q] = f2_fma(e2, qw, acc[q]);
+      c2 = f2_fma(e2, xi2[q], c2);
     }
-    col[b] = c;
+    float c0, c1;
+    f2_unpack(c2, c0, c1);
+    col[b] = c0 + c1;
   }
 #pragma unroll
-  for (int a = 0; a < 4; ++a) rowbuf[warp][lane + 32 * a] = acc_r[a];
+  for (int q = 0; q < 2; ++q) {
+    float a0, a1;
+    f2_unpack(acc[q], a0, a1);
+    rowbuf[warp][lane + 64 * q] = a0;
+    rowbuf[warp][lane + 64 * q + 32] = a1;
+  }
   if (I != J) {
     warp_reduce_scatter32(col, lane);
     S[((long long)J * T + I) * kB + 32 * warp + lane] = col[0];

@@ -66,6 +66,8 @@ def lib():
         L.orc_bicgstab.restype = I
         L.orc_true_relres.argtypes = [C.POINTER(Operator), P, P]
         L.orc_true_relres.restype = D
+        L.orc_true_relres_accurate.argtypes = [C.POINTER(Operator), P, P]
+        L.orc_true_relres_accurate.restype = D
         L.orc_apply.argtypes = [C.POINTER(Operator), P, P]
         L.orc_save_vector.argtypes = [C.c_char_p, I, P]
         L.orc_load_vector.argtypes = [C.c_char_p, I, P]
@@ -158,6 +160,12 @@ def bicgstab(op, b, x0=None, iter_max=1000, eps=1e-10, history=False):
 def true_relres(op, b, x) -> float:
     b, x = _f64(b), _f64(x)
     return lib().orc_true_relres(C.byref(op.op), b.ctypes.data, x.ctypes.data)
+
+
+def true_relres_accurate(op, b, x) -> float:
+    """||b - A x|| / ||b|| with compensated (double-double) residual entries."""
+    b, x = _f64(b), _f64(x)
+    return lib().orc_true_relres_accurate(C.byref(op.op), b.ctypes.data, x.ctypes.data)
 
 
 def save_vector(path: str, x) -> int:

@@ -283,6 +283,50 @@ double orc_true_relres(const orc_operator* op, const double* b, const double* x)
   return sqrt(rr) / sqrt(bb);
 }
 
+/* ||b - A x|| / ||b|| with each residual entry b_i - sum_j A_ij x_j formed in
+ * double-double arithmetic (products split exactly by fma, sums by TwoSum):
+ * the compensated dot product Dot2 of Ogita, Rump and Oishi ("Accurate sum
+ * and dot product", SIAM J. Sci. Comput. 26(6), 2005), with b_i as the first
+ * summand.  The only errors left are those of the FP64 entries A_ij, so the
+ * value does not carry the summation noise u * sum_j |A_ij x_j| that a plain
+ * FP64 residual has on ill-conditioned kernel systems. */
+static inline void two_sum(double a, double b, double* s, double* e) {
+  const double t = a + b;
+  const double bp = t - a;
+  *e = (a - (t - bp)) + (b - bp);
+  *s = t;
+}
+
+static double residual_entry(const orc_operator* op, const double* b, const double* x, int i) {
+  double s = b[i], c = 0.0;
+  for (int j = 0; j < op->n; ++j) {
+    double a;
+    if (op->kind == ORC_OP_DENSE)
+      a = op->A[(long)j * op->lda + i];
+    else
+      a = (op->rule == ORC_RULE_KERNEL_CU) ? orc_gauss_entry_kernelcu(op->coords, op->ld, op->dim, i, j)
+                                           : orc_gauss_entry_assembler(op->coords, op->ld, op->dim, i, j, op->nugget);
+    const double p = -a * x[j];
+    const double pe = fma(-a, x[j], -p);
+    double e;
+    two_sum(s, p, &s, &e);
+    c += e + pe;
+  }
+  return s + c;
+}
+
+double orc_true_relres_accurate(const orc_operator* op, const double* b, const double* x) {
+  const int n = op->n;
+  double rr = 0.0, bb = 0.0;
+#pragma omp parallel for reduction(+ : rr, bb) schedule(dynamic, 16)
+  for (int i = 0; i < n; ++i) {
+    const double t = residual_entry(op, b, x, i);
+    rr += t * t;
+    bb += b[i] * b[i];
+  }
+  return sqrt(rr) / sqrt(bb);
+}
+
 /* Operator matvec exposed for the checker. */
 void orc_apply(const orc_operator* op, const double* x, double* y) { mv(op, x, y); }
 

@@ -38,6 +38,7 @@ int orc_cg(const orc_operator* op, const double* b, double* x, int iter_max, dou
 int orc_bicgstab(const orc_operator* op, const double* b, double* x, int iter_max, double eps, double* final_res,
                  int* status, double* hist);
 double orc_true_relres(const orc_operator* op, const double* b, const double* x);
+double orc_true_relres_accurate(const orc_operator* op, const double* b, const double* x);
 void orc_apply(const orc_operator* op, const double* x, double* y);
 int orc_save_vector(const char* path, int n, const double* x);
 int orc_load_vector(const char* path, int n, double* x);

@@ -3,8 +3,10 @@ half FP64 and half mixed, are admitted while others run, all finish at the
 FP64 tolerance, and a request's result is bitwise the same when it is solved
 alone as when it was served in the mix.
 
-The oracle's FP64 recomputation of the residual gets the same 50% slack as
-in the batch tests (x reaches about 1e4 ||b|| on these systems)."""
+Residual checks use the oracle's double-double residual with the bounds of
+the batch tests: 1.2e-10 for mixed requests (which certify 1e-10 on their
+own double-double true residual), 1e-8 for FP64 requests (which stop on the
+recursive residual like the reference's CG)."""
 import time
 
 import numpy as np
@@ -44,9 +46,10 @@ def test_served_results_are_correct_and_match_solo_solves(gpu, orc):
         c = by_id[req.rid]
         op = orc.GaussOp(req.points, req.nugget)
         for j in range(req.b.shape[1]):
-            assert c.infos[j].status == 0
+            assert c.infos[j].status == 0, (req.rid, req.precision, c.infos[j].as_dict())
             assert c.infos[j].final_res < 1e-10
-            assert orc.true_relres(op, req.b[:, j], c.x[:, j]) < 1.5e-10
+            tol = 1.2e-10 if req.precision == 1 else 1e-8
+            assert orc.true_relres_accurate(op, req.b[:, j], c.x[:, j]) < tol
     for req in reqs[:2]:
         solo = gpu.Batch(2)
         h = solo.add(req.points, req.nugget, req.b, precision=req.precision, iter_max=200000)

@@ -135,3 +135,25 @@ def test_oracle_vector_file_format(orc, tmp_path):
     st, y = orc.load_vector(p, 17)
     assert st == 0 and np.array_equal(x, y)
     assert orc.load_vector(p, 16)[0] == -2
+
+
+def test_oracle_accurate_residual_is_exact_where_plain_fp64_is_not(orc):
+    # Columns come in pairs (a v, -a v) with integer products below 2^52,
+    # shuffled apart, plus one column of ones with x = 1 and b = 1: the exact
+    # residual is 0.  Double-double residual entries recover it exactly; a
+    # plain FP64 residual of the same data carries summation noise.
+    rng = np.random.default_rng(5)
+    pairs, n = 32, 64
+    a = rng.integers(1 << 24, 1 << 26, size=(n, pairs)).astype(np.float64)
+    v = rng.integers(1 << 24, 1 << 26, size=pairs).astype(np.float64)
+    A = np.zeros((n, 2 * pairs + 1))
+    A[:, 0:2 * pairs:2] = a
+    A[:, 1:2 * pairs:2] = -a
+    A[:, -1] = 1.0
+    x = np.concatenate([np.repeat(v, 2), [1.0]])
+    perm = rng.permutation(2 * pairs + 1)
+    A, x = A[:, perm], x[perm]
+    op = orc.DenseOp(np.asfortranarray(np.vstack([A, np.zeros((1, 2 * pairs + 1))])))
+    b = np.concatenate([np.ones(n), [0.0]])
+    assert orc.true_relres_accurate(op, b, x) == 0.0
+    assert orc.true_relres(op, b, x) > 1e-3
