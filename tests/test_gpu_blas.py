@@ -63,6 +63,30 @@ def test_dgemv_matches_oracle(gpu, orc, m, n, lda, off):
     assert rel_err(got, want, A, x) <= TOL
 
 
+@pytest.mark.parametrize("x_out_of_range", [False, True])
+def test_dgemv_wide_magnitudes(gpu, orc, x_out_of_range):
+    # the products run as FP32 pairs for |a|, |x| in [2^-50, 2^58); elements
+    # outside (zeros, subnormals, 1e-300, 1e100) and CTAs whose x has such an
+    # entry take FP64 FMAs -- every mix must meet the same bar
+    rng = np.random.default_rng(11)
+    m, n = 1500, 2100
+    A = rng.uniform(-1, 1, (m, n)) * 10.0 ** rng.integers(-20, 20, (m, n))
+    pick = rng.random((m, n))
+    A[pick < 0.05] = 0.0
+    A[(pick >= 0.05) & (pick < 0.06)] = 1e-300
+    A[(pick >= 0.06) & (pick < 0.07)] = -1e100
+    A[(pick >= 0.07) & (pick < 0.075)] = 5e-320  # subnormal
+    A = np.asfortranarray(A)
+    x = rng.uniform(-1, 1, n) * 10.0 ** rng.integers(-10, 10, n)
+    x[::7] = 0.0
+    if x_out_of_range:
+        x[5] = 3e-200
+        x[1900] = 1e80
+    got = run_dgemv(gpu, A, x)
+    want = orc.dgemv(A, x)
+    assert rel_err(got, want, A, x) <= TOL
+
+
 def test_dgemv_is_bit_reproducible(gpu):
     rng = np.random.default_rng(11)
     A = np.asfortranarray(rng.standard_normal((2048, 3000)))
