@@ -9,21 +9,29 @@
 //
 // One step (captured once into a CUDA graph, replayed until every lane is
 // done):
-//   mv32    persistent kernel over (system, 128-row tile) items of mixed
-//           systems: z = K~ d, entries in FP32 with the exponential on the
-//           SFU, 128-column partial sums in FP32 added into FP64
-//   mv64    persistent kernel over items of FP64 systems: z = K d in FP64
-//   alpha   one CTA per system: alpha_k = <r,r>_k / <d,z>_k
-//   update  one CTA per system: x += alpha d, r -= alpha z, new <r,r>; mixed
-//           lanes decide whether the FP64 true residual is due
-//   mv64r   persistent kernel over items of mixed systems with a pending
-//           replacement: z = b - K x in double-double (returns at once
-//           otherwise)
-//   replace one CTA per system: r = z for those lanes, convergence test
-//           on the FP64 true residual, restart of the direction
-//   dir     one CTA per system: d = beta d + r (and its FP32 copy)
-// Systems and item lists live in device memory, so systems are added and
-// retired between replays (the serving loop) without re-capturing.
+//   mv32    persistent kernel over (system, 128 rows, 2048-column chunk)
+//           items of mixed systems: partial K~ d per chunk, entries in FP32
+//           with the exponential on the SFU, 128-column sums in FP32 added
+//           into FP64
+//   mv64    the same items of FP64 systems: partial K d in FP64
+//   alpha   persistent kernel over (system, 1024-row) items: z = nugget d +
+//           the chunk partials in chunk order, per-item <d,z>; the last item
+//           of a system to finish sums the items in order and sets alpha
+//   update  x += alpha d, r -= alpha z, <r,r>; the last item sets beta, the
+//           stop test, and for mixed lanes whether the FP64 true residual is
+//           due
+//   mv64r   (system, 128 rows) items of mixed systems with a pending
+//           replacement: z = b - K x, FP64 entries, each 128-column tile
+//           summed in FP64 and the tile sums in double-double
+//   replace r = z for those lanes, convergence test on the FP64 true
+//           residual, restart of the direction
+//   dir     d = beta d + r (and its FP32 copy)
+//   count   lanes still running per system, systems still running
+// Work is split so that one large system still spreads over the whole GPU,
+// and every sum runs in an order fixed by the system's own size: a system's
+// result is bitwise the same alone and in any mix.  Systems and item lists
+// live in device memory, so systems are added and retired between replays
+// (the serving loop) without re-capturing.
 //
 // Mixed precision.  K~ is the FP32 operator: coordinates are carried as an
 // FP32 pair (hi, lo) so that a coordinate difference is accurate to FP32
@@ -53,7 +61,9 @@ namespace {
 
 constexpr int kTile = 128;        // rows per item and threads per matvec CTA
 constexpr int kColTile = 128;     // columns staged per shared-memory round
-constexpr int kVecThreads = 256;  // per-system vector kernels
+constexpr int kChunkCols = 2048;  // columns per matvec item
+constexpr int kVecThreads = 256;  // threads of the vector-phase CTAs
+constexpr int kVecRows = 1024;    // rows per vector-phase item
 
 enum LaneDone : int { LANE_RUNNING = 0, LANE_CONVERGED = 1, LANE_CAPPED = 2, LANE_BROKE = 3 };
 enum QueueMode : int { Q_MV32 = 0, Q_MV64 = 1, Q_MV64_TRUE = 2 };
@@ -127,8 +137,8 @@ __device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
   return r;
 }
 
-// z = K~ d + nugget d for the R lanes of mixed systems of one class.  A
-// thread owns RPT rows (RPT/2 packed pairs: rows r and r + 128 of a pair of
+// Partial (K~ d) over one column chunk for the R lanes of mixed systems of one
+// class, into P[chunk].  A thread owns RPT rows (RPT/2 packed pairs: rows r and r + 128 of a pair of
 // tiles); column values are staged in shared memory twice over so that one
 // load gives a packed operand.  Coordinate differences are
 // fl(fl(hi_i - hi_j) + fl(lo_i - lo_j)): exact-symmetric and accurate to the
@@ -172,8 +182,9 @@ __global__ void __launch_bounds__(kTile) k_bmv32(WorkQueue q, const BatchSys* __
     for (int a = 0; a < RPT; ++a)
 #pragma unroll
       for (int k = 0; k < R; ++k) acc[a][k] = 0.0;
-    for (int j0 = 0; j0 < n; j0 += kColTile) {
-      const int nj = min(kColTile, n - j0);
+    const int c0 = w.chunk * kChunkCols, c1 = min(n, c0 + kChunkCols);
+    for (int j0 = c0; j0 < c1; j0 += kColTile) {
+      const int nj = min(kColTile, c1 - j0);
       __syncthreads();
       for (int t = threadIdx.x; t < kColTile; t += kTile) {
         const bool in = t < nj;
@@ -243,10 +254,7 @@ __global__ void __launch_bounds__(kTile) k_bmv32(WorkQueue q, const BatchSys* __
     for (int a = 0; a < RPT; ++a) {
       if (row[a] < n) {
 #pragma unroll
-        for (int k = 0; k < R; ++k) {
-          const long long o = (long long)row[a] * R + k;
-          S.z[o] = fma(S.nugget, S.d[o], acc[a][k]);
-        }
+        for (int k = 0; k < R; ++k) S.P[((long long)w.chunk * n + row[a]) * R + k] = acc[a][k];
       }
     }
   }
@@ -254,20 +262,21 @@ __global__ void __launch_bounds__(kTile) k_bmv32(WorkQueue q, const BatchSys* __
 }
 
 // ------------------------------------------------------- FP64 matvec
-// TRUE_RES = false: z = K d + nugget d for FP64 systems (the reference's
-// FP64 iteration).  TRUE_RES = true: z = b - (K x + nugget x), the true
-// residual of mixed systems with a pending replacement, with every row's sum
-// kept in double-double (products split exactly by fma, sums by TwoSum: the
-// compensated dot product of Ogita, Rump and Oishi).  On these systems x
-// reaches ~1e4 ||b|| and a plain FP64 sum of K_ij x_j carries noise of about
-// u * sum_j |K_ij x_j|, i.e. ~1e-10 relative: the very tolerance the mixed
-// iteration must certify.
-__device__ __forceinline__ void dd_add(double& s, double& c, double p, double pe) {
+// TRUE_RES = false: partial K d over one column chunk of FP64 systems, into
+// P[chunk] (the reference's FP64 iteration).  TRUE_RES = true: the true
+// residual z = b - (K x + nugget x) of mixed systems with a pending
+// replacement, whole rows (the chunk-0 items only).  On these systems x
+// reaches ~1e4 ||b||, and a plain FP64 sum of K_ij x_j over a whole row
+// carries noise of about u * sum_j |K_ij x_j|, i.e. ~1e-10 relative: the
+// very tolerance the mixed iteration must certify.  So each 128-column tile
+// is summed in FP64 (its terms are local) and the tile sums are added in
+// double-double (TwoSum: Knuth, TAOCP vol. 2, 4.2.2).
+__device__ __forceinline__ void dd_add(double& s, double& c, double p) {
   const double t = __dadd_rn(s, p);
   const double bp = __dsub_rn(t, s);
   const double e = __dadd_rn(__dsub_rn(s, __dsub_rn(t, bp)), __dsub_rn(p, bp));
   s = t;
-  c = __dadd_rn(c, __dadd_rn(e, pe));
+  c = __dadd_rn(c, e);
 }
 
 template <int DIM, int R, bool TRUE_RES>
@@ -285,18 +294,20 @@ __global__ void __launch_bounds__(kTile) k_bmv64(WorkQueue q, const BatchSys* __
     const BatchSys& S = sys[w.sys];
     if (!sys_active(S) || S.dim != DIM || S.R != R) continue;
     if (!TRUE_RES && S.precision != MGB_PREC_FP64) continue;
-    if (TRUE_RES && (S.precision != MGB_PREC_MIXED || !S.need_hi)) continue;
+    if (TRUE_RES && (S.precision != MGB_PREC_MIXED || !S.need_hi || w.chunk != 0)) continue;
     const int n = S.n;
     const double* v = TRUE_RES ? S.x : S.d;
     const int i = w.row0 + threadIdx.x;
+    const int c0 = TRUE_RES ? 0 : w.chunk * kChunkCols;
+    const int c1 = TRUE_RES ? n : min(n, c0 + kChunkCols);
     double pi[DIM];
 #pragma unroll
     for (int d = 0; d < DIM; ++d) pi[d] = S.pts64[(long long)d * n + min(i, n - 1)];
     double acc[R], cmp[R];
 #pragma unroll
     for (int k = 0; k < R; ++k) acc[k] = cmp[k] = 0.0;
-    for (int j0 = 0; j0 < n; j0 += kColTile) {
-      const int nj = min(kColTile, n - j0);
+    for (int j0 = c0; j0 < c1; j0 += kColTile) {
+      const int nj = min(kColTile, c1 - j0);
       __syncthreads();
       for (int t = threadIdx.x; t < kColTile; t += kTile) {
         const bool in = t < nj;
@@ -306,6 +317,9 @@ __global__ void __launch_bounds__(kTile) k_bmv64(WorkQueue q, const BatchSys* __
         for (int k = 0; k < R; ++k) sv[t * R + k] = in ? v[(long long)(j0 + t) * R + k] : 0.0;
       }
       __syncthreads();
+      double tile[R];
+#pragma unroll
+      for (int k = 0; k < R; ++k) tile[k] = 0.0;
       for (int t = 0; t < nj; ++t) {
         double s = 0.0;
 #pragma unroll
@@ -315,15 +329,12 @@ __global__ void __launch_bounds__(kTile) k_bmv64(WorkQueue q, const BatchSys* __
         }
         const double e = exp_neg_table(s, table);
 #pragma unroll
-        for (int k = 0; k < R; ++k) {
-          const double vk = sv[t * R + k];
-          if (TRUE_RES) {
-            const double p = __dmul_rn(e, vk);
-            dd_add(acc[k], cmp[k], p, fma(e, vk, -p));
-          } else {
-            acc[k] = fma(e, vk, acc[k]);
-          }
-        }
+        for (int k = 0; k < R; ++k) tile[k] = fma(e, sv[t * R + k], tile[k]);
+      }
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        if (TRUE_RES) dd_add(acc[k], cmp[k], tile[k]);
+        else acc[k] += tile[k];
       }
     }
     if (i < n) {
@@ -331,13 +342,11 @@ __global__ void __launch_bounds__(kTile) k_bmv64(WorkQueue q, const BatchSys* __
       for (int k = 0; k < R; ++k) {
         const long long o = (long long)i * R + k;
         if (TRUE_RES) {
-          const double p = __dmul_rn(S.nugget, v[o]);
-          dd_add(acc[k], cmp[k], p, fma(S.nugget, v[o], -p));
-          // b - (acc + cmp): b and acc agree to a few digits, so b - acc is
-          // exact or nearly so
+          dd_add(acc[k], cmp[k], S.nugget * v[o]);
+          // b and acc agree to a few digits, so b - acc is (nearly) exact
           S.z[o] = __dsub_rn(__dsub_rn(S.b[o], acc[k]), cmp[k]);
         } else {
-          S.z[o] = fma(S.nugget, v[o], acc[k]);
+          S.P[((long long)w.chunk * n + i) * R + k] = acc[k];
         }
       }
     }
@@ -345,9 +354,10 @@ __global__ void __launch_bounds__(kTile) k_bmv64(WorkQueue q, const BatchSys* __
   queue_done(q);
 }
 
-// ---------------------------------------------------- per-system kernels
-// Block-wide sums of R per-thread values (one per lane); every thread gets
-// the totals.  Fixed order, so results do not depend on other systems.
+// ---------------------------------------------------------- vector phases
+// Persistent kernels over (system, kVecRows rows) items.  Each item writes
+// its R partial sums to S.vpart in item order; the last item of a system to
+// arrive sums them in that order and runs the lane scalars.
 template <int R>
 __device__ __forceinline__ void block_sums(double (&v)[R], double* smem) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -372,27 +382,53 @@ __device__ __forceinline__ void block_sums(double (&v)[R], double* smem) {
   __syncthreads();
 }
 
+// Writes this item's partials, and returns true in the last item of the
+// system with tot[k] = the system-wide sums (item order).
 template <int R>
-__device__ void vec_alpha(BatchSys& S, double* smem) {
+__device__ bool finish_item(BatchSys& S, int vi, double (&v)[R], double* smem, int* s_last, double (&tot)[8]) {
+  block_sums<R>(v, smem);
+  if (threadIdx.x < R) S.vpart[vi * 8 + threadIdx.x] = v[threadIdx.x];
+  if (!last_block_arrival(S.ticket, (unsigned)S.nvec, s_last)) return false;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) tot[k] = 0.0;
+  for (int c = 0; c < S.nvec; ++c)
+#pragma unroll
+    for (int k = 0; k < R; ++k) tot[k] += __ldcg(&S.vpart[c * 8 + k]);
+  return true;
+}
+
+template <int R>
+__device__ void vec_alpha(BatchSys& S, int row0, double* smem, int* s_last) {
   double v[R];
 #pragma unroll
   for (int k = 0; k < R; ++k) v[k] = 0.0;
-  for (int i = threadIdx.x; i < S.n; i += kVecThreads)
+  const int n = S.n, row1 = min(n, row0 + kVecRows);
+  for (int i = row0 + threadIdx.x; i < row1; i += kVecThreads) {
 #pragma unroll
-    for (int k = 0; k < R; ++k) v[k] = fma(S.d[(long long)i * R + k], S.z[(long long)i * R + k], v[k]);
-  block_sums<R>(v, smem);
+    for (int k = 0; k < R; ++k) {
+      const long long o = (long long)i * R + k;
+      double z = 0.0;
+      for (int c = 0; c < S.nchunks; ++c) z += S.P[(long long)c * n * R + o];
+      const double dv = S.d[o];
+      z = fma(S.nugget, dv, z);
+      S.z[o] = z;
+      v[k] = fma(dv, z, v[k]);
+    }
+  }
+  double tot[8];
+  if (!finish_item<R>(S, row0 / kVecRows, v, smem, s_last, tot)) return;
   if (threadIdx.x < R) {
     BatchLane& L = S.lanes[threadIdx.x];
     if (L.done == LANE_RUNNING) {
-      const double a = L.rr / v[threadIdx.x];
-      if (!(v[threadIdx.x] > 0.0) || !isfinite(a)) L.done = LANE_BROKE;
+      const double a = L.rr / tot[threadIdx.x];
+      if (!(tot[threadIdx.x] > 0.0) || !isfinite(a)) L.done = LANE_BROKE;
       else L.alpha = a;
     }
   }
 }
 
 template <int R>
-__device__ void vec_update(BatchSys& S, double* smem, double delta2) {
+__device__ void vec_update(BatchSys& S, int row0, double* smem, int* s_last, double delta2) {
   __shared__ double s_alpha[8];
   __shared__ int s_run[8];
   if (threadIdx.x < R) {
@@ -403,7 +439,8 @@ __device__ void vec_update(BatchSys& S, double* smem, double delta2) {
   double v[R];
 #pragma unroll
   for (int k = 0; k < R; ++k) v[k] = 0.0;
-  for (int i = threadIdx.x; i < S.n; i += kVecThreads) {
+  const int row1 = min(S.n, row0 + kVecRows);
+  for (int i = row0 + threadIdx.x; i < row1; i += kVecThreads) {
 #pragma unroll
     for (int k = 0; k < R; ++k) {
       const long long o = (long long)i * R + k;
@@ -415,14 +452,15 @@ __device__ void vec_update(BatchSys& S, double* smem, double delta2) {
       }
     }
   }
-  block_sums<R>(v, smem);
+  double tot[8];
+  if (!finish_item<R>(S, row0 / kVecRows, v, smem, s_last, tot)) return;
   if (threadIdx.x == 0) {
     int need = 0;
     for (int k = 0; k < R; ++k) {
       BatchLane& L = S.lanes[k];
       if (L.done != LANE_RUNNING) continue;
       L.k += 1;
-      const double rr_new = v[k];
+      const double rr_new = tot[k];
       if (S.precision == MGB_PREC_MIXED) {
         const bool replace = (rr_new < delta2 * L.rr_ref) || (sqrt(rr_new) / L.bnorm < S.eps) ||
                              (L.k + 1 >= S.iter_max) || !(rr_new == rr_new);
@@ -448,34 +486,35 @@ __device__ void vec_update(BatchSys& S, double* smem, double delta2) {
 }
 
 template <int R>
-__device__ void vec_replace(BatchSys& S, double* smem) {
-  if (S.precision != MGB_PREC_MIXED || !S.need_hi) return;
+__device__ void vec_replace(BatchSys& S, int row0, double* smem, int* s_last) {
   __shared__ int s_flag[8];
   if (threadIdx.x < R) s_flag[threadIdx.x] = S.lanes[threadIdx.x].done == LANE_RUNNING && S.lanes[threadIdx.x].flag;
   __syncthreads();
   double v[R];
 #pragma unroll
   for (int k = 0; k < R; ++k) v[k] = 0.0;
-  for (int i = threadIdx.x; i < S.n; i += kVecThreads) {
+  const int row1 = min(S.n, row0 + kVecRows);
+  for (int i = row0 + threadIdx.x; i < row1; i += kVecThreads) {
 #pragma unroll
     for (int k = 0; k < R; ++k) {
       if (!s_flag[k]) continue;
       const long long o = (long long)i * R + k;
-      const double ri = S.z[o];  // b - K x from the double-double matvec
+      const double ri = S.z[o];  // b - K x from the true-residual matvec
       S.r[o] = ri;
       v[k] = fma(ri, ri, v[k]);
     }
   }
-  block_sums<R>(v, smem);
+  double tot[8];
+  if (!finish_item<R>(S, row0 / kVecRows, v, smem, s_last, tot)) return;
   if (threadIdx.x == 0) {
     for (int k = 0; k < R; ++k) {
       if (!s_flag[k]) continue;
       BatchLane& L = S.lanes[k];
-      L.res = sqrt(v[k]) / L.bnorm;
+      L.res = sqrt(tot[k]) / L.bnorm;
       L.replacements += 1;
       L.beta = 0.0;  // restart the direction from the true residual
-      L.rr = v[k];
-      L.rr_ref = v[k];
+      L.rr = tot[k];
+      L.rr_ref = tot[k];
       L.flag = 0;
       if (L.res < S.eps) L.done = LANE_CONVERGED;
       else if (!(L.res == L.res)) L.done = LANE_BROKE;
@@ -486,7 +525,7 @@ __device__ void vec_replace(BatchSys& S, double* smem) {
 }
 
 template <int R>
-__device__ void vec_direction(BatchSys& S) {
+__device__ void vec_direction(BatchSys& S, int row0) {
   __shared__ double s_beta[8];
   __shared__ int s_run[8];
   if (threadIdx.x < R) {
@@ -494,7 +533,8 @@ __device__ void vec_direction(BatchSys& S) {
     s_run[threadIdx.x] = S.lanes[threadIdx.x].done == LANE_RUNNING;
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < S.n; i += kVecThreads) {
+  const int row1 = min(S.n, row0 + kVecRows);
+  for (int i = row0 + threadIdx.x; i < row1; i += kVecThreads) {
 #pragma unroll
     for (int k = 0; k < R; ++k) {
       const long long o = (long long)i * R + k;
@@ -503,42 +543,46 @@ __device__ void vec_direction(BatchSys& S) {
       if (S.d32) S.d32[o] = (float)dn;
     }
   }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int act = 0;
-    for (int k = 0; k < R; ++k) act += S.lanes[k].done == LANE_RUNNING;
-    S.active_lanes = act;
-  }
 }
 
-// One kernel per phase, one CTA per system slot; the R dispatch is a
-// runtime switch over templated bodies.
+// One persistent kernel per phase; the R dispatch is a runtime switch over
+// templated bodies.  Phase 2 (replace) touches only systems with a pending
+// true residual; every item of such a system takes part, so the last-arrival
+// count is complete.
 template <int PHASE>
-__global__ void __launch_bounds__(kVecThreads) k_bvec(BatchSys* sys, int nslots, double delta2) {
+__global__ void __launch_bounds__(kVecThreads) k_bvec(WorkQueue q, const VecItem* __restrict__ vitems,
+                                                      BatchSys* sys, double delta2) {
   __shared__ double smem[80];
-  const int sidx = blockIdx.x;
-  if (sidx >= nslots) return;
-  BatchSys& S = sys[sidx];
-  if (!sys_active(S)) return;
-  switch (S.R) {
-#define MGB_BVEC_CASE(RR)                            \
-  case RR:                                           \
-    if (PHASE == 0) vec_alpha<RR>(S, smem);          \
-    if (PHASE == 1) vec_update<RR>(S, smem, delta2); \
-    if (PHASE == 2) vec_replace<RR>(S, smem);        \
-    if (PHASE == 3) vec_direction<RR>(S);            \
+  __shared__ int s_item, s_last;
+  for (;;) {
+    const int it = claim(q, &s_item);
+    if (it >= *q.count) break;
+    const VecItem w = vitems[it];
+    BatchSys& S = sys[w.sys];
+    if (!sys_active(S)) continue;
+    if (PHASE == 2 && (S.precision != MGB_PREC_MIXED || !S.need_hi)) continue;
+    switch (S.R) {
+#define MGB_BVEC_CASE(RR)                                             \
+  case RR:                                                            \
+    if (PHASE == 0) vec_alpha<RR>(S, w.row0, smem, &s_last);          \
+    if (PHASE == 1) vec_update<RR>(S, w.row0, smem, &s_last, delta2); \
+    if (PHASE == 2) vec_replace<RR>(S, w.row0, smem, &s_last);        \
+    if (PHASE == 3) vec_direction<RR>(S, w.row0);                     \
     break;
-    MGB_BVEC_CASE(1)
-    MGB_BVEC_CASE(2)
-    MGB_BVEC_CASE(4)
-    MGB_BVEC_CASE(8)
+      MGB_BVEC_CASE(1)
+      MGB_BVEC_CASE(2)
+      MGB_BVEC_CASE(4)
+      MGB_BVEC_CASE(8)
 #undef MGB_BVEC_CASE
-    default:
-      break;
+      default:
+        break;
+    }
   }
+  queue_done(q);
 }
 
-// Initial state with x0 = 0: r = d = b, <r,r> and ||b|| per lane.
+// Initial state with x0 = 0: r = d = b, <r,r> and ||b|| per lane (one CTA,
+// once per admitted system).
 __global__ void __launch_bounds__(kVecThreads) k_binit(BatchSys* sys, int slot) {
   __shared__ double smem[80];
   BatchSys& S = sys[slot];
@@ -572,13 +616,22 @@ __global__ void __launch_bounds__(kVecThreads) k_binit(BatchSys* sys, int slot) 
     }
     S.active_lanes = act;
     S.need_hi = 0;
+    *S.ticket = 0u;
   }
 }
 
-__global__ void k_bcount(const BatchSys* sys, int nslots, int* active) {
+// End of a step: lanes still running per system, systems still running.
+__global__ void k_bcount(BatchSys* sys, int nslots, int* active) {
   __shared__ int sm[32];
   int a = 0;
-  for (int s = threadIdx.x; s < nslots; s += blockDim.x) a += sys_active(sys[s]) ? 1 : 0;
+  for (int s = threadIdx.x; s < nslots; s += blockDim.x) {
+    BatchSys& S = sys[s];
+    if (!S.in_use) continue;
+    int act = 0;
+    for (int k = 0; k < S.R; ++k) act += S.lanes[k].done == LANE_RUNNING;
+    S.active_lanes = act;
+    a += act > 0 ? 1 : 0;
+  }
   a = __reduce_add_sync(0xffffffffu, a);
   if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = a;
   __syncthreads();
@@ -602,11 +655,13 @@ int BatchEngine::init(DeviceContext* c, int max_systems, cudaStream_t s) {
   blocks_.assign(max_systems, nullptr);
   MGB_TRY(pool_alloc(c, sizeof(BatchSys) * max_systems, (void**)&dev_sys_));
   MGB_CUDA(cudaMemsetAsync(dev_sys_, 0, sizeof(BatchSys) * max_systems, s));
-  max_items_ = 1 << 16;
+  max_items_ = 1 << 18;
   for (int q = 0; q < kClasses; ++q) {
     MGB_TRY(pool_alloc(c, sizeof(BatchItem) * max_items_, (void**)&items_[q]));
     items_host_[q].clear();
   }
+  MGB_TRY(pool_alloc(c, sizeof(VecItem) * max_items_, (void**)&vitems_));
+  vitems_host_.clear();
   MGB_TRY(pool_alloc(c, sizeof(int) * kCounterInts, (void**)&counters_));
   MGB_CUDA(cudaMemsetAsync(counters_, 0, sizeof(int) * kCounterInts, s));
   MGB_CUDA(cudaMallocHost(&active_host_, sizeof(int)));
@@ -622,6 +677,7 @@ BatchEngine::~BatchEngine() {
     if (host_[i].in_use) release_slot(i);
   for (int q = 0; q < kClasses; ++q)
     if (items_[q]) pool_free(c_, items_[q]);
+  if (vitems_) pool_free(c_, vitems_);
   if (counters_) pool_free(c_, counters_);
   if (dev_sys_) pool_free(c_, dev_sys_);
   if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
@@ -634,11 +690,18 @@ int BatchEngine::class_of(int dim, int R) {
   return (dim == 2 ? 0 : 4) + r;
 }
 
+static int chunks_of(int n) { return (n + kChunkCols - 1) / kChunkCols; }
+static int vec_items_of(int n) { return (n + kVecRows - 1) / kVecRows; }
+
 size_t BatchEngine::bytes_needed(int n, int dim, int nrhs, int precision) {
   const int R = padded_rhs(nrhs);
   const size_t nv = (size_t)n * R;
-  size_t b = 5 * (sizeof(double) * nv + 256) + sizeof(double) * (size_t)n * dim + 256 + sizeof(BatchLane) * 8 + 256;
-  if (precision == MGB_PREC_MIXED) b += 2 * (sizeof(float4) * (size_t)n + 256) + sizeof(float) * nv + 256;
+  const size_t pad = 256;
+  size_t b = 5 * (sizeof(double) * nv + pad) + sizeof(double) * (size_t)n * dim + pad + sizeof(BatchLane) * 8 + pad;
+  b += sizeof(double) * nv * chunks_of(n) + pad;        // matvec partials
+  b += sizeof(double) * 8 * vec_items_of(n) + pad;      // vector-phase partials
+  b += sizeof(unsigned int) + pad;                      // ticket
+  if (precision == MGB_PREC_MIXED) b += 2 * (sizeof(float4) * (size_t)n + pad) + sizeof(float) * nv + pad;
   return b;
 }
 
@@ -657,9 +720,11 @@ int BatchEngine::add(int n, int dim, const double* coords_host, double nugget, i
   if (slot < 0) return set_error(MGB_ERR_NOMEM, "batch add: all %d system slots in use", max_);
   const int R = padded_rhs(nrhs);
   const int cls = class_of(dim, R);
-  const int new_items = (n + kTile - 1) / kTile;
-  if ((int)items_host_[cls].size() + new_items > max_items_)
-    return set_error(MGB_ERR_NOMEM, "batch add: more than %d work items in one class", max_items_);
+  const int nchunks = chunks_of(n), nvec = vec_items_of(n);
+  const long long new_items = (long long)((n + kTile - 1) / kTile) * nchunks;
+  if ((long long)items_host_[cls].size() + new_items > max_items_ ||
+      (long long)vitems_host_.size() + nvec > max_items_)
+    return set_error(MGB_ERR_NOMEM, "batch add: more than %d work items", max_items_);
   // admission by free device memory
   const size_t need = bytes_needed(n, dim, nrhs, precision);
   size_t free_b = 0, total_b = 0;
@@ -677,6 +742,8 @@ int BatchEngine::add(int n, int dim, const double* coords_host, double nugget, i
   S.iter_max = iter_max;
   S.eps = eps;
   S.nugget = nugget;
+  S.nchunks = nchunks;
+  S.nvec = nvec;
   char* base = nullptr;
   MGB_TRY(pool_alloc(c_, need, (void**)&base));
   blocks_[slot] = base;
@@ -691,6 +758,9 @@ int BatchEngine::add(int n, int dim, const double* coords_host, double nugget, i
   S.d = (double*)take(sizeof(double) * nv);
   S.z = (double*)take(sizeof(double) * nv);
   S.b = (double*)take(sizeof(double) * nv);
+  S.P = (double*)take(sizeof(double) * nv * nchunks);
+  S.vpart = (double*)take(sizeof(double) * 8 * nvec);
+  S.ticket = (unsigned int*)take(sizeof(unsigned int));
   S.pts64 = (const double*)take(sizeof(double) * (size_t)n * dim);
   S.lanes = (BatchLane*)take(sizeof(BatchLane) * 8);
   if (precision == MGB_PREC_MIXED) {
@@ -730,7 +800,9 @@ int BatchEngine::add(int n, int dim, const double* coords_host, double nugget, i
   MGB_CUDA(cudaGetLastError());
   // the host staging buffers must outlive the async copies
   MGB_CUDA(cudaStreamSynchronize(s_));
-  for (int r0 = 0; r0 < n; r0 += kTile) items_host_[cls].push_back(BatchItem{slot, r0});
+  for (int r0 = 0; r0 < n; r0 += kTile)
+    for (int c = 0; c < nchunks; ++c) items_host_[cls].push_back(BatchItem{slot, r0, c});
+  for (int r0 = 0; r0 < n; r0 += kVecRows) vitems_host_.push_back(VecItem{slot, r0});
   items_dirty_ = true;
   nslots_ = std::max(nslots_, slot + 1);
   *handle = slot;
@@ -743,6 +815,9 @@ void BatchEngine::release_slot(int slot) {
   const int cls = class_of(host_[slot].dim, host_[slot].R);
   auto& v = items_host_[cls];
   v.erase(std::remove_if(v.begin(), v.end(), [&](const BatchItem& w) { return w.sys == slot; }), v.end());
+  vitems_host_.erase(std::remove_if(vitems_host_.begin(), vitems_host_.end(),
+                                    [&](const VecItem& w) { return w.sys == slot; }),
+                     vitems_host_.end());
   host_[slot] = BatchSys{};
   items_dirty_ = true;
 }
@@ -756,21 +831,25 @@ int BatchEngine::sync_items() {
                                s_));
     count_host_[q] = cnt;
   }
-  MGB_CUDA(cudaMemcpyAsync(counters_ + 6 * kClasses, count_host_, sizeof(int) * kClasses, cudaMemcpyHostToDevice,
-                           s_));
+  vcount_host_ = (int)vitems_host_.size();
+  if (vcount_host_)
+    MGB_CUDA(cudaMemcpyAsync(vitems_, vitems_host_.data(), sizeof(VecItem) * vcount_host_, cudaMemcpyHostToDevice,
+                             s_));
+  MGB_CUDA(cudaMemcpyAsync(counters_ + kOffCount, count_host_, sizeof(int) * kClasses, cudaMemcpyHostToDevice, s_));
+  MGB_CUDA(cudaMemcpyAsync(counters_ + kOffVecCount, &vcount_host_, sizeof(int), cudaMemcpyHostToDevice, s_));
   MGB_CUDA(cudaStreamSynchronize(s_));
   items_dirty_ = false;
   return MGB_OK;
 }
 
-// counters_ layout: [class][mode] -> (claim, finished) at (cls * 3 + mode) * 2,
-// item counts at 6 * kClasses + cls, active systems at 7 * kClasses.
-static WorkQueue make_queue(const BatchItem* items, int* counters, int cls, int mode, int classes) {
+// Matvec queue of class `cls` and mode: (claim, finished) counters at
+// kOffMv + (cls * 3 + mode) * 2, item count at kOffCount + cls.
+static WorkQueue make_queue(const BatchItem* items, int* counters, int cls, int mode) {
   WorkQueue q;
   q.items = items;
-  q.count = counters + 6 * classes + cls;
-  q.counter = counters + (cls * 3 + mode) * 2;
-  q.finished = reinterpret_cast<unsigned int*>(counters + (cls * 3 + mode) * 2 + 1);
+  q.count = counters + BatchEngine::kOffCount + cls;
+  q.counter = counters + BatchEngine::kOffMv + (cls * 3 + mode) * 2;
+  q.finished = reinterpret_cast<unsigned int*>(q.counter + 1);
   return q;
 }
 
@@ -781,7 +860,7 @@ static void launch_mv32(const WorkQueue& q, const BatchSys* sys, int rpt, int gr
 }
 
 int BatchEngine::enqueue_mv32(int cls, int rpt) {
-  const WorkQueue q = make_queue(items_[cls], counters_, cls, Q_MV32, kClasses);
+  const WorkQueue q = make_queue(items_[cls], counters_, cls, Q_MV32);
   const int grid = 4 * c_->num_sms;
   switch (cls) {
     case 0: launch_mv32<2, 1>(q, dev_sys_, rpt, grid, s_); break;
@@ -806,7 +885,7 @@ static void launch_mv64(const WorkQueue& q, const BatchSys* sys, bool true_res, 
 }
 
 int BatchEngine::enqueue_mv64(int cls, int mode) {
-  const WorkQueue q = make_queue(items_[cls], counters_, cls, mode, kClasses);
+  const WorkQueue q = make_queue(items_[cls], counters_, cls, mode);
   const int grid = 2 * c_->num_sms;
   const double* t = c_->exp_table;
   const bool tr = mode == Q_MV64_TRUE;
@@ -825,22 +904,39 @@ int BatchEngine::enqueue_mv64(int cls, int mode) {
   return MGB_OK;
 }
 
-int BatchEngine::enqueue_step() {
+int BatchEngine::enqueue_vec(int phase) {
+  WorkQueue q;
+  q.items = nullptr;
+  q.count = counters_ + kOffVecCount;
+  q.counter = counters_ + kOffVec + 2 * phase;
+  q.finished = reinterpret_cast<unsigned int*>(q.counter + 1);
+  const int grid = 2 * c_->num_sms;
   const double delta2 = 1e-4;  // replacement when the recursive residual fell 100x
+  switch (phase) {
+    case 0: k_bvec<0><<<grid, kVecThreads, 0, s_>>>(q, vitems_, dev_sys_, delta2); break;
+    case 1: k_bvec<1><<<grid, kVecThreads, 0, s_>>>(q, vitems_, dev_sys_, delta2); break;
+    case 2: k_bvec<2><<<grid, kVecThreads, 0, s_>>>(q, vitems_, dev_sys_, delta2); break;
+    default: k_bvec<3><<<grid, kVecThreads, 0, s_>>>(q, vitems_, dev_sys_, delta2); break;
+  }
+  count_launches(1);
+  MGB_CUDA(cudaGetLastError());
+  return MGB_OK;
+}
+
+int BatchEngine::enqueue_step() {
   for (int cls = 0; cls < kClasses; ++cls) {
     if (!count_host_[cls]) continue;
     MGB_TRY(enqueue_mv32(cls, rpt_[cls] ? rpt_[cls] : 2));
     MGB_TRY(enqueue_mv64(cls, Q_MV64));
   }
-  k_bvec<0><<<nslots_, kVecThreads, 0, s_>>>(dev_sys_, nslots_, delta2);
-  k_bvec<1><<<nslots_, kVecThreads, 0, s_>>>(dev_sys_, nslots_, delta2);
-  count_launches(2);
+  MGB_TRY(enqueue_vec(0));
+  MGB_TRY(enqueue_vec(1));
   for (int cls = 0; cls < kClasses; ++cls)
     if (count_host_[cls]) MGB_TRY(enqueue_mv64(cls, Q_MV64_TRUE));
-  k_bvec<2><<<nslots_, kVecThreads, 0, s_>>>(dev_sys_, nslots_, delta2);
-  k_bvec<3><<<nslots_, kVecThreads, 0, s_>>>(dev_sys_, nslots_, delta2);
-  k_bcount<<<1, 256, 0, s_>>>(dev_sys_, nslots_, counters_ + 7 * kClasses);
-  count_launches(3);
+  MGB_TRY(enqueue_vec(2));
+  MGB_TRY(enqueue_vec(3));
+  k_bcount<<<1, 256, 0, s_>>>(dev_sys_, nslots_, counters_ + kOffActive);
+  count_launches(1);
   MGB_CUDA(cudaGetLastError());
   return MGB_OK;
 }
@@ -921,7 +1017,7 @@ int BatchEngine::run_steps(int steps, int* active_out) {
     MGB_CUDA(cudaGraphLaunch(graph_exec_, s_));
     count_launches(graph_kernels_);
     done_steps += kStepsPerGraph;
-    MGB_CUDA(cudaMemcpyAsync(active_host_, counters_ + 7 * kClasses, sizeof(int), cudaMemcpyDeviceToHost, s_));
+    MGB_CUDA(cudaMemcpyAsync(active_host_, counters_ + kOffActive, sizeof(int), cudaMemcpyDeviceToHost, s_));
     MGB_CUDA(cudaStreamSynchronize(s_));
     active = *active_host_;
   }

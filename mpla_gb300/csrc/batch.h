@@ -29,11 +29,16 @@ struct BatchSys {
   int n, dim, R, nrhs;
   int precision;     // MGB_PREC_FP64 or MGB_PREC_MIXED
   int iter_max;
-  int active_lanes;  // lanes still running
+  int active_lanes;  // lanes still running (updated at the end of a step)
   int need_hi;       // mixed: some lane needs the FP64 true residual this step
+  int nchunks;       // column chunks of the matvec items
+  int nvec;          // row chunks of the vector phases
   int pad;
   double eps, nugget;
   double *x, *r, *d, *z, *b;
+  double* P;             // matvec partials: nchunks x n x R (chunk-major)
+  double* vpart;         // vector-phase partial sums: nvec x 8
+  unsigned int* ticket;  // last-arrival counter of the vector phases
   const double* pts64;   // dim x n, structure of arrays
   const float4* pts_hi;  // mixed: coordinates x sqrt(log2 e), rounded to FP32 ...
   const float4* pts_lo;  // ... and the FP32 remainder (hi + lo carries ~48 bits)
@@ -41,8 +46,15 @@ struct BatchSys {
   BatchLane* lanes;      // 8 lanes
 };
 
-// A work item of the persistent matvec kernels: 128 rows of one system.
+// Matvec work item: 128 rows x one column chunk of one system.
 struct BatchItem {
+  int sys;
+  int row0;
+  int chunk;
+};
+
+// Vector-phase work item: a chunk of rows of one system.
+struct VecItem {
   int sys;
   int row0;
 };
@@ -51,9 +63,15 @@ class BatchEngine {
  public:
   static constexpr int kClasses = 8;        // (dim 2|3) x (R 1|2|4|8)
   static constexpr int kStepsPerGraph = 8;  // CG iterations per graph replay
-  // counters: per class and mode, (claim counter, finished counter, pad);
-  // then the item counts per class; then the active-system count
-  static constexpr int kCounterInts = 6 * kClasses + kClasses + 4;
+  // device counters: matvec queues (claim, finished) per class and mode,
+  // item counts per class, the active-system count, vector-phase queues
+  // (claim, finished) per phase and the vector item count
+  static constexpr int kOffMv = 0;
+  static constexpr int kOffCount = 6 * kClasses;
+  static constexpr int kOffActive = 7 * kClasses;
+  static constexpr int kOffVec = 7 * kClasses + 1;
+  static constexpr int kOffVecCount = kOffVec + 8;
+  static constexpr int kCounterInts = kOffVecCount + 4;
 
   ~BatchEngine();
   int init(DeviceContext* c, int max_systems, cudaStream_t s);
@@ -74,6 +92,7 @@ class BatchEngine {
   int enqueue_step();
   int enqueue_mv32(int cls, int rpt);
   int enqueue_mv64(int cls, int mode);
+  int enqueue_vec(int phase);
 
   DeviceContext* c_ = nullptr;
   cudaStream_t s_ = nullptr;
@@ -85,6 +104,9 @@ class BatchEngine {
   BatchItem* items_[kClasses] = {};
   std::vector<BatchItem> items_host_[kClasses];
   int count_host_[kClasses] = {};
+  VecItem* vitems_ = nullptr;
+  std::vector<VecItem> vitems_host_;
+  int vcount_host_ = 0;
   int max_items_ = 0;
   bool items_dirty_ = false;
   int* counters_ = nullptr;
