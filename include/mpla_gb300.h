@@ -152,6 +152,17 @@ int mgb_cg_gauss_host(int n, int dim, const double* coords_host, double nugget,
                       const double* b_host, double* x_host, int iter_max, double eps,
                       int precision, mgb_solve_info* info);
 
+/* Kernel of the mixed-precision Gaussian matvec, for matvecs and solvers set
+ * up after the call (no counterpart in the reference):
+ *   MGB_MIXED_TENSOR  squared distances as a split-BF16 tcgen05 contraction,
+ *                     exponentials on the SFU (sm_103a tensor cores);
+ *   MGB_MIXED_SIMT    squared distances from FP32 coordinate differences.
+ * Both are symmetric FP32 operators of the same kernel matrix. */
+#define MGB_MIXED_TENSOR 0
+#define MGB_MIXED_SIMT 1
+int mgb_set_mixed_matvec(int kind);
+int mgb_get_mixed_matvec(void);
+
 /* ------------------------------------------------------------ measurement */
 /* Kernels this library has launched so far in this process (a kernel node
  * replayed by a CUDA graph counts once per replay). */

@@ -32,6 +32,8 @@ STOP_RELATIVE = 0
 STOP_RMS = 1
 PREC_FP64 = 0
 PREC_MIXED = 1
+MIXED_TENSOR = 0
+MIXED_SIMT = 1
 
 # Every C-ABI symbol declared in include/mpla_gb300.h (checked by the tests).
 C_ABI_SYMBOLS = (
@@ -45,6 +47,7 @@ C_ABI_SYMBOLS = (
     "mgb_save_vector", "mgb_load_vector",
     "mgb_batch_create", "mgb_batch_add", "mgb_batch_run", "mgb_batch_finished", "mgb_batch_result",
     "mgb_batch_tuning", "mgb_batch_destroy",
+    "mgb_set_mixed_matvec", "mgb_get_mixed_matvec",
 )
 
 
@@ -112,6 +115,8 @@ _SIGS = {
     "mgb_batch_result": (_I, [_P, _I, _P, C.POINTER(SolveInfo), _I]),
     "mgb_batch_tuning": (_I, [_P, _P, _P]),
     "mgb_batch_destroy": (_I, [_P]),
+    "mgb_set_mixed_matvec": (_I, [_I]),
+    "mgb_get_mixed_matvec": (_I, []),
 }
 
 
@@ -248,6 +253,16 @@ def gauss_entries(pts: GaussPoints, i: np.ndarray, j: np.ndarray, nugget=0.0, ru
     check(lib().mgb_gauss_entries_f64(pts.n, di.count, di.ptr, dj.ptr, pts.dim, pts.coords, float(nugget), rule,
                                       out.ptr, None))
     return out.numpy()
+
+
+def set_mixed_matvec(kind: int) -> None:
+    """Kernel of the mixed-precision matvec (MIXED_TENSOR or MIXED_SIMT) for
+    matvecs and solvers set up afterwards."""
+    check(lib().mgb_set_mixed_matvec(int(kind)))
+
+
+def get_mixed_matvec() -> int:
+    return int(lib().mgb_get_mixed_matvec())
 
 
 def kernel_launches() -> int:

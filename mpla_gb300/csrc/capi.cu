@@ -1,3 +1,4 @@
+#include <atomic>
 // C ABI of the hot path (mpla_gb300.h): dense BLAS, Gaussian matvecs and the
 // solver entry points, plus the Matvec adapters the solvers run on.
 #include <cmath>
@@ -41,8 +42,17 @@ int GaussF64Matvec::apply(const double* x, double* y, cudaStream_t s, const int*
 
 GaussMixedMatvec::~GaussMixedMatvec() { delete impl_; }
 
+namespace {
+std::atomic<int> g_mixed_kind{MGB_MIXED_SIMT};
+}
+
 int GaussMixedMatvec::init(DeviceContext* c, const GaussSystem& g, cudaStream_t s) {
   n_ = g.rows;
+  if (g_mixed_kind.load() == MGB_MIXED_TENSOR) {
+    SymTC* m = new SymTC();
+    impl_ = m;
+    return m->init(c, g, s);
+  }
   SymF32* m = new SymF32();
   impl_ = m;
   return m->init(c, g, s);
@@ -296,6 +306,15 @@ int mgb_time_gauss_matvec(int n, int dim, const double* const* coords, double nu
   MGB_TRY(A.init(c, g, s));
   return time_launches(s, reps, ms_per_launch, [&]() { return A.apply(x, y, s, nullptr); });
 }
+
+int mgb_set_mixed_matvec(int kind) {
+  if (kind != MGB_MIXED_TENSOR && kind != MGB_MIXED_SIMT)
+    return set_error(MGB_ERR_ARG, "unknown mixed matvec kind %d", kind);
+  g_mixed_kind.store(kind);
+  return MGB_OK;
+}
+
+int mgb_get_mixed_matvec(void) { return g_mixed_kind.load(); }
 
 int mgb_time_dgemv(int n, const double* A, const double* x, double* y, int reps, double* ms_per_launch,
                    void* stream) {

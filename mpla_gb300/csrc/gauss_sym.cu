@@ -398,6 +398,33 @@ uint64_t spread2(uint64_t v) {
 // ---------------------------------------------------------------- host side
 int sym_tiles(int n) { return (n + kB - 1) / kB; }
 
+std::vector<int> morton_perm(const std::vector<double>& h, int n, int dim) {
+  double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  for (int d = 0; d < dim; ++d) {
+    lo[d] = hi[d] = h[(size_t)d * n];
+    for (int i = 0; i < n; ++i) {
+      lo[d] = std::min(lo[d], h[(size_t)d * n + i]);
+      hi[d] = std::max(hi[d], h[(size_t)d * n + i]);
+    }
+  }
+  std::vector<uint64_t> key(n);
+  for (int i = 0; i < n; ++i) {
+    uint64_t q[3] = {0, 0, 0};
+    for (int d = 0; d < dim; ++d) {
+      const double span = hi[d] > lo[d] ? hi[d] - lo[d] : 1.0;
+      const double u = (h[(size_t)d * n + i] - lo[d]) / span;
+      const double bits = dim == 3 ? 2097151.0 : 4294967295.0;
+      q[d] = (uint64_t)std::min(bits, std::max(0.0, u * bits));
+    }
+    key[i] = dim == 3 ? (spread3(q[0]) | spread3(q[1]) << 1 | spread3(q[2]) << 2)
+                      : (dim == 2 ? (spread2(q[0]) | spread2(q[1]) << 1) : q[0]);
+  }
+  std::vector<int> perm(n);
+  std::iota(perm.begin(), perm.end(), 0);
+  std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) { return key[a] < key[b]; });
+  return perm;
+}
+
 SymF64::~SymF64() {
   if (c_) pool_free(c_, S_);
 }
@@ -451,29 +478,7 @@ int SymF32::init(DeviceContext* c, const GaussSystem& g, cudaStream_t s) {
     MGB_CUDA(cudaMemcpyAsync(h.data() + (size_t)d * n_, g.coords[d], sizeof(double) * n_, cudaMemcpyDeviceToHost, s));
   MGB_CUDA(cudaStreamSynchronize(s));
   const double scale = std::sqrt(1.4426950408889634);  // sqrt(log2 e): exp(-s) = 2^(-s log2 e)
-  double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
-  for (int d = 0; d < dim_; ++d) {
-    lo[d] = hi[d] = h[(size_t)d * n_];
-    for (int i = 0; i < n_; ++i) {
-      lo[d] = std::min(lo[d], h[(size_t)d * n_ + i]);
-      hi[d] = std::max(hi[d], h[(size_t)d * n_ + i]);
-    }
-  }
-  std::vector<uint64_t> key(n_);
-  for (int i = 0; i < n_; ++i) {
-    uint64_t q[3] = {0, 0, 0};
-    for (int d = 0; d < dim_; ++d) {
-      const double span = hi[d] > lo[d] ? hi[d] - lo[d] : 1.0;
-      const double u = (h[(size_t)d * n_ + i] - lo[d]) / span;
-      const double bits = dim_ == 3 ? 2097151.0 : 4294967295.0;
-      q[d] = (uint64_t)std::min(bits, std::max(0.0, u * bits));
-    }
-    key[i] = dim_ == 3 ? (spread3(q[0]) | spread3(q[1]) << 1 | spread3(q[2]) << 2)
-                       : (dim_ == 2 ? (spread2(q[0]) | spread2(q[1]) << 1) : q[0]);
-  }
-  std::vector<int> perm(n_);
-  std::iota(perm.begin(), perm.end(), 0);
-  std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) { return key[a] < key[b]; });
+  const std::vector<int> perm = morton_perm(h, n_, dim_);
   // Tile centres stay zero (global coordinates): see the FP32 note at the
   // top of the file.
   std::vector<double> centers((size_t)3 * T_, 0.0);

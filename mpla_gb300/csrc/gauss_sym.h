@@ -1,11 +1,16 @@
 // Symmetric tile-pair Gaussian matvecs (gauss_sym.cu) for square systems.
 #pragma once
 
+#include <vector>
+
 #include "internal.h"
 
 namespace mgb {
 
 int sym_tiles(int n);
+// Morton (Z-order) permutation of n points (dim x n, structure of arrays):
+// sorted position -> original index.
+std::vector<int> morton_perm(const std::vector<double>& h, int n, int dim);
 
 // FP64: the plain-CG operator.
 class SymF64 : public Matvec {
@@ -39,6 +44,32 @@ class SymF32 : public Matvec {
   int* perm_ = nullptr;       // sorted position -> original index
   float* S_ = nullptr;        // T x T x 128 slot partials (pool block, also holds xf_)
   float* xf_ = nullptr;       // x gathered into sorted order, FP32
+};
+
+// FP32 + SFU with the squared distances as a BF16 tensor-core contraction
+// (gauss_tc.cu): the default mixed-CG operator.
+class SymTC : public Matvec {
+ public:
+  ~SymTC() override;
+  int init(DeviceContext* c, const GaussSystem& g, cudaStream_t s);
+  int apply(const double* x, double* y, cudaStream_t s, const int* skip) override;
+  int n() const override { return n_; }
+
+ private:
+  DeviceContext* c_ = nullptr;
+  int n_ = 0, dim_ = 0, T_ = 0, GT_ = 0;
+  long long ncta_ = 0;
+  double nugget_ = 0.0;
+  void* block_ = nullptr;           // pool block holding the arrays below
+  unsigned char* btiles_ = nullptr; // T column-tile operands (BF16, canonical layout)
+  float4* phi_ = nullptr;           // scaled coordinates, FP32 high part (Morton order, whole tiles)
+  float4* plo_ = nullptr;           // ... and low part
+  float4* ctr_ = nullptr;           // tile centres (FP32)
+  int2* map_ = nullptr;             // CTA -> (column tile, row-tile pair)
+  int* perm_ = nullptr;             // sorted position -> original index
+  float* S_ = nullptr;              // row slots T x T x 128, then column slots, then xf
+  float* Scol_ = nullptr;           // column slots T x GT x 128
+  float* xf_ = nullptr;             // x gathered into sorted order, FP32
 };
 
 }  // namespace mgb

@@ -44,3 +44,13 @@ def orc():
 
     oracle.lib()
     return oracle
+
+
+@pytest.fixture(params=[0, 1], ids=["tensor", "simt"])
+def mixed_kind(gpu, request):
+    """Run a mixed-precision test with each matvec kernel (MIXED_TENSOR,
+    MIXED_SIMT), restoring the library-wide choice afterwards."""
+    old = gpu.get_mixed_matvec()
+    gpu.set_mixed_matvec(request.param)
+    yield request.param
+    gpu.set_mixed_matvec(old)

@@ -3,7 +3,8 @@
 FP64 kernel: entries within 4 ulp of the oracle's libm exp (the table method
 is about 1 ulp; the oracle goes through sqrt then squares, as the reference
 does), matvec within 1e-13 relative to sum_j |K_ij x_j|.
-Mixed kernel: FP32 arithmetic and ex2.approx, within 2e-5 relative.
+Mixed kernels (tensor-core distances and FP32 differences): FP32 arithmetic
+and ex2.approx, within 2e-5 relative, bit-reproducible.
 """
 import numpy as np
 import pytest
@@ -97,8 +98,8 @@ def test_fp64_far_points_underflow_to_zero(gpu):
     assert got[1] == 0.0 and got[2] == 0.0
 
 
-@pytest.mark.parametrize("n,dim,ell", [(100, 1, 0.05), (4096, 2, 0.05), (5000, 3, 0.08)])
-def test_mixed_matvec_close_to_oracle(gpu, orc, n, dim, ell):
+@pytest.mark.parametrize("n,dim,ell", [(100, 1, 0.05), (300, 3, 0.1), (4096, 2, 0.05), (5000, 3, 0.08)])
+def test_mixed_matvec_close_to_oracle(gpu, orc, mixed_kind, n, dim, ell):
     pts = scaled_points(n, dim, ell, seed=n + 1)
     x = np.random.default_rng(n).standard_normal(n)
     dp = gpu.GaussPoints(pts)
@@ -117,6 +118,20 @@ def test_fp64_matvec_is_bit_reproducible(gpu):
     for _ in range(2):
         dy = gpu.DeviceArray(6000)
         gpu.gauss_matvec_f64(dp, 1e-4, gpu.NUGGET_DIAGONAL, dx.ptr, dy.ptr)
+        gpu.synchronize()
+        outs.append(dy.numpy())
+    assert np.array_equal(outs[0], outs[1])
+
+
+def test_mixed_matvec_is_bit_reproducible(gpu, mixed_kind):
+    pts = scaled_points(3000, 3, 0.1, seed=3)
+    x = np.random.default_rng(3).standard_normal(3000)
+    dp = gpu.GaussPoints(pts)
+    dx = gpu.DeviceArray.from_numpy(x)
+    outs = []
+    for _ in range(2):
+        dy = gpu.DeviceArray(3000)
+        gpu.gauss_matvec_mixed(dp, 1e-4, dx.ptr, dy.ptr)
         gpu.synchronize()
         outs.append(dy.numpy())
     assert np.array_equal(outs[0], outs[1])

@@ -99,7 +99,7 @@ def test_cg_gauss_fp64_matches_oracle(gpu, orc, n, dim, ell, nug, band):
 
 
 @pytest.mark.parametrize("n,dim,ell", [(1024, 2, 0.05), (2000, 3, 0.08), (4096, 2, 0.05)])
-def test_cg_gauss_mixed_reaches_fp64_tolerance(gpu, orc, n, dim, ell):
+def test_cg_gauss_mixed_reaches_fp64_tolerance(gpu, orc, mixed_kind, n, dim, ell):
     pts = scaled(n, dim, ell, seed=4)
     b = synth.sincos_rhs(synth.gauss_points(n, dim, 4))
     dp = gpu.GaussPoints(pts)
