@@ -21,8 +21,8 @@
 //           stop test, and for mixed lanes whether the FP64 true residual is
 //           due
 //   mv64r   (system, 128 rows) items of mixed systems with a pending
-//           replacement: z = b - K x, FP64 entries, each 128-column tile
-//           summed in FP64 and the tile sums in double-double
+//           replacement: z = b - K x, FP64 entries, products and sums in
+//           double-double
 //   replace r = z for those lanes, convergence test on the FP64 true
 //           residual, restart of the direction
 //   dir     d = beta d + r (and its FP32 copy)
@@ -266,17 +266,19 @@ __global__ void __launch_bounds__(kTile) k_bmv32(WorkQueue q, const BatchSys* __
 // P[chunk] (the reference's FP64 iteration).  TRUE_RES = true: the true
 // residual z = b - (K x + nugget x) of mixed systems with a pending
 // replacement, whole rows (the chunk-0 items only).  On these systems x
-// reaches ~1e4 ||b||, and a plain FP64 sum of K_ij x_j over a whole row
-// carries noise of about u * sum_j |K_ij x_j|, i.e. ~1e-10 relative: the
-// very tolerance the mixed iteration must certify.  So each 128-column tile
-// is summed in FP64 (its terms are local) and the tile sums are added in
-// double-double (TwoSum: Knuth, TAOCP vol. 2, 4.2.2).
-__device__ __forceinline__ void dd_add(double& s, double& c, double p) {
+// reaches ~1e4 ||b||, and a plain FP64 sum of K_ij x_j over a row carries
+// noise of about u * sum_j |K_ij x_j|, i.e. ~1e-10 relative: the very
+// tolerance the mixed iteration must certify (points are in the caller's
+// order, so even a 128-column tile mixes far-apart large terms).  So every
+// product is split exactly by an FMA and summed in double-double (TwoSum,
+// Knuth, TAOCP vol. 2, 4.2.2): the compensated dot product of Ogita, Rump
+// and Oishi.
+__device__ __forceinline__ void dd_add(double& s, double& c, double p, double pe) {
   const double t = __dadd_rn(s, p);
   const double bp = __dsub_rn(t, s);
   const double e = __dadd_rn(__dsub_rn(s, __dsub_rn(t, bp)), __dsub_rn(p, bp));
   s = t;
-  c = __dadd_rn(c, e);
+  c = __dadd_rn(c, __dadd_rn(e, pe));
 }
 
 template <int DIM, int R, bool TRUE_RES>
@@ -329,20 +331,27 @@ __global__ void __launch_bounds__(kTile) k_bmv64(WorkQueue q, const BatchSys* __
         }
         const double e = exp_neg_table(s, table);
 #pragma unroll
-        for (int k = 0; k < R; ++k) tile[k] = fma(e, sv[t * R + k], tile[k]);
+        for (int k = 0; k < R; ++k) {
+          const double vk = sv[t * R + k];
+          if (TRUE_RES) {
+            const double p = __dmul_rn(e, vk);
+            dd_add(acc[k], cmp[k], p, fma(e, vk, -p));
+          } else {
+            tile[k] = fma(e, vk, tile[k]);
+          }
+        }
       }
+      if (!TRUE_RES)
 #pragma unroll
-      for (int k = 0; k < R; ++k) {
-        if (TRUE_RES) dd_add(acc[k], cmp[k], tile[k]);
-        else acc[k] += tile[k];
-      }
+        for (int k = 0; k < R; ++k) acc[k] += tile[k];
     }
     if (i < n) {
 #pragma unroll
       for (int k = 0; k < R; ++k) {
         const long long o = (long long)i * R + k;
         if (TRUE_RES) {
-          dd_add(acc[k], cmp[k], S.nugget * v[o]);
+          const double p = __dmul_rn(S.nugget, v[o]);
+          dd_add(acc[k], cmp[k], p, fma(S.nugget, v[o], -p));
           // b and acc agree to a few digits, so b - acc is (nearly) exact
           S.z[o] = __dsub_rn(__dsub_rn(S.b[o], acc[k]), cmp[k]);
         } else {
