@@ -3,7 +3,8 @@
 //
 // 8 bytes of A per 2 flops: HBM-bound on paper, but GB300 issues only ~2
 // FP64 FMAs per clock per SM, which at n = 4096 takes longer than streaming A.
-// So the products run in FP32 pairs with FP64 accuracy:
+// So most products run in FP32 pairs with FP64 accuracy, beside FP64 FMAs on
+// the rest (3 columns of every 8), keeping both kinds of pipe busy:
 //   * each matrix element a is split exactly by integer operations into
 //     ah (its top 24 significand bits, a float) and al (the other 29 bits,
 //     converted to float: 2^-53 relative error), x likewise once per CTA;
@@ -141,36 +142,64 @@ __global__ void __launch_bounds__(kThreads) dgemv_kernel(int m, int n, const dou
   }
   const bool use_split = !__syncthreads_or(bad);
   if (x_ready && use_split && r < m && wc0 < wc1) {
+    // Columns 0-2 of every group of 8 take FP64 FMAs and columns 3-7 the
+    // FP32-pair products, so the FP64 pipe and the FP32/integer pipes work
+    // side by side (each alone would take longer than streaming A).  The
+    // next group's loads are issued before the current group is computed.
     const double* a = A + (long long)(col0 + wc0) * lda + r;
     const bool pair = (VEC == 2) && (r + 1 < m);
     float S0 = 0.f, C0 = 0.f, S1 = 0.f, C1 = 0.f;
     int j = wc0;
-    for (; j + 8 <= wc1; j += 8) {
-      if (VEC == 2 && pair) {
-        double2 v[8];
+    if (VEC == 2 && pair) {
+      double2 v[8];
+      if (j + 8 <= wc1) {
 #pragma unroll
         for (int u = 0; u < 8; ++u) v[u] = ld_stream2(a + (long long)u * lda);
+      }
+      for (; j + 8 <= wc1; j += 8) {
+        double2 nv[8];
+        const bool more = j + 16 <= wc1;
+        if (more) {
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
+          for (int u = 0; u < 8; ++u) nv[u] = ld_stream2(a + (long long)(8 + u) * lda);
+        }
+#pragma unroll
+        for (int u = 0; u < 3; ++u) {
+          const double x64 = xs[j + u];
+          acc0 = fma(v[u].x, x64, acc0);
+          acc1 = fma(v[u].y, x64, acc1);
+        }
+#pragma unroll
+        for (int u = 3; u < 8; ++u) {
           const float2 xv = xsp[j + u];
           const double x64 = xs[j + u];
           split_fma(v[u].x, xv.x, xv.y, x64, S0, C0, acc0);
           split_fma(v[u].y, xv.x, xv.y, x64, S1, C1, acc1);
         }
-      } else {
+        a += 8 * lda;
+        if (((j - wc0) & 63) == 56) {  // every 64 columns
+          split_flush(S0, C0, acc0);
+          split_flush(S1, C1, acc1);
+        }
+        if (more) {
+#pragma unroll
+          for (int u = 0; u < 8; ++u) v[u] = nv[u];
+        }
+      }
+    } else {
+      for (; j + 8 <= wc1; j += 8) {
         double v[8];
 #pragma unroll
         for (int u = 0; u < 8; ++u) v[u] = ld_stream1(a + (long long)u * lda);
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
+        for (int u = 0; u < 3; ++u) acc0 = fma(v[u], xs[j + u], acc0);
+#pragma unroll
+        for (int u = 3; u < 8; ++u) {
           const float2 xv = xsp[j + u];
           split_fma(v[u], xv.x, xv.y, xs[j + u], S0, C0, acc0);
         }
-      }
-      a += 8 * lda;
-      if (((j - wc0) & 63) == 56) {  // every 64 columns
-        split_flush(S0, C0, acc0);
-        split_flush(S1, C1, acc1);
+        a += 8 * lda;
+        if (((j - wc0) & 63) == 56) split_flush(S0, C0, acc0);
       }
     }
     for (; j < wc1; ++j) {
@@ -276,10 +305,10 @@ int launch_dgemv(DeviceContext* c, int m, int n, const double* A, int lda, const
   const int rows_per_strip = vec2 ? 64 : 32;
   const int strips = (m + rows_per_strip - 1) / rows_per_strip;
   // Columns per warp: enough CTAs to cover the machine several times over,
-  // at least 16 columns per warp so each thread keeps 8 loads in flight.
+  // at least 64 columns per warp, so the per-CTA staging of x is amortised.
   int cpw = 128;
   const long long target = 6LL * c->num_sms;
-  while (cpw > 16 && (long long)strips * ((n + kWarps * cpw - 1) / (kWarps * cpw)) < target) cpw >>= 1;
+  while (cpw > 64 && (long long)strips * ((n + kWarps * cpw - 1) / (kWarps * cpw)) < target) cpw >>= 1;
   const int nsplit = (n + kWarps * cpw - 1) / (kWarps * cpw);
   if (nsplit > 1) {
     MGB_TRY(ensure_split_partials(c, (size_t)nsplit * m));
