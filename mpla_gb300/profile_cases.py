@@ -6,6 +6,8 @@ that ends by itself (a few hundred MB on the device at most):
   python -m mpla_gb300.profile_cases dgemv       # dense dgemv, n = 4096 (134 MB matrix)
   python -m mpla_gb300.profile_cases gauss_f64   # FP64 Gaussian matvec, n = 16384, d = 2
   python -m mpla_gb300.profile_cases gauss_mixed # FP32/SFU Gaussian matvec, n = 65536, d = 2
+  python -m mpla_gb300.profile_cases mixed_cg    # 300 mixed-CG iterations, n = 16384, d = 2
+  python -m mpla_gb300.profile_cases batch       # 100 steps of a 24-system batch (n <= 4096)
   python -m mpla_gb300.profile_cases all
 
 Prints the CUDA-event time per launch of each case.
@@ -48,7 +50,35 @@ def case_gauss_mixed(reps=3):
     _gauss(65536, 2, 0.05, mg.PREC_MIXED, reps)
 
 
-CASES = {"dgemv": case_dgemv, "gauss_f64": case_gauss_f64, "gauss_mixed": case_gauss_mixed}
+def case_mixed_cg(iters=300):
+    """The headline solve's kernel mix (FP32 matvec, fused vector kernels,
+    FP64 true residuals) on the n = 16384 member of its family, capped at
+    `iters` iterations so that a launch list stays short."""
+    n = 16384
+    prob = synth.gauss_problem(n, 2, 0.05, 1e-4, seed=0)
+    dp = mg.GaussPoints(prob.scaled())
+    b = mg.DeviceArray.from_numpy(prob.b)
+    x = mg.DeviceArray(n)
+    x.zero()
+    info = mg.cg_gauss(dp, 1e-4, b.ptr, x.ptr, iter_max=iters, eps=1e-10, precision=mg.PREC_MIXED)
+    print(f"mixed_cg n={n}: {info.iterations} iterations, relres {info.true_relres:.3e}")
+
+
+def case_batch(steps=100):
+    """The batched engine's kernel mix: 24 systems of the batch workload with
+    n <= 4096, advanced by `steps` iterations."""
+    spec = synth.batch_spec(24, n_hi=4096)
+    batch = mg.Batch(24)
+    for k in range(24):
+        g = synth.batch_system(spec, k)
+        batch.add(g.scaled(), g.nugget, g.b, precision=mg.PREC_MIXED)
+    active = batch.run(max_steps=steps)
+    print(f"batch: {active} of 24 systems still running after {steps} steps")
+    batch.close()
+
+
+CASES = {"dgemv": case_dgemv, "gauss_f64": case_gauss_f64, "gauss_mixed": case_gauss_mixed,
+         "mixed_cg": case_mixed_cg, "batch": case_batch}
 
 
 def main(argv):
