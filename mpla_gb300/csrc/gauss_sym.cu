@@ -246,100 +246,114 @@ __device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
   return r;
 }
 
-// Per column t of tile J the shared arrays hold each value twice, so that one
-// 128-bit load gives packed operands: cq[t] = {x, x, y, y},
-// cw[t] = {z, z, x_t, x_t} (x_t the FP32 vector entry).  Lane l's rows pair
-// up as (l, l+32) and (l+64, l+96).  Per pair of entries: two packed
-// subtractions (three for d = 3), a packed multiply and FMA for the squared
-// distance, two MUFU.EX2, a packed FMA into the row sums and one into the
-// column partial -- the same arithmetic, entry for entry, as the scalar form
-// fl(fl(dx^2 + fl(dy^2))) with dx = fl(x_i - x_j).
+// One CTA takes a column tile J and a group of up to kGroup row tiles
+// I = kGroup*g .. min(kGroup*g + kGroup - 1, J).  The column tile is staged
+// once in shared memory with each value twice over, so that one 128-bit load
+// gives packed operands: cq[t] = {x, x, y, y}, cw[t] = {z, z, x_t, x_t} (x_t
+// the FP32 vector entry).  Warp w owns columns 32w .. 32w+31 and, for every
+// row tile of the group, lane l owns rows l, l+32, l+64, l+96, paired as
+// (l, l+32) and (l+64, l+96).  Per pair of entries: packed subtractions, a
+// packed multiply and FMA for the squared distance, two MUFU.EX2, a packed
+// FMA into the row sums and one into the column partial.  Column partials
+// accumulate over the whole group in registers, and one butterfly
+// reduce-scatter per CTA (31 shuffles and adds per lane) leaves lane l with
+// column 32w + l complete (the warp saw every row of the group).  The
+// diagonal tile I = J is evaluated in full for its row sums and adds nothing
+// to the column partials (its row weights are zero there), so every
+// unordered pair of points counts once per direction.  Row sums of each row
+// tile combine the 4 warps in shared memory in warp order.
+constexpr int kGroup = 4;
+
 template <int DIM>
-__global__ void __launch_bounds__(kF32Threads) sym_f32_pair_kernel(int n, int T, const float4* __restrict__ pts,
-                                                                   const double* __restrict__ centers,
-                                                                   const float* __restrict__ xf,
-                                                                   float* __restrict__ S,
-                                                                   const int* __restrict__ skip) {
+__global__ void __launch_bounds__(kF32Threads) sym_f32_group_kernel(int n, int T, int GT,
+                                                                    const int2* __restrict__ map,
+                                                                    const float4* __restrict__ pts,
+                                                                    const float* __restrict__ xf,
+                                                                    float* __restrict__ Srow,
+                                                                    float* __restrict__ Scol,
+                                                                    const int* __restrict__ skip) {
   if (skip && *skip) return;
-  __shared__ float4 sr[kB];
   __shared__ float4 cq[kB];
   __shared__ float4 cw[kB];
-  __shared__ float rowbuf[4][kB];
-  __shared__ float s_dc[3];
-  int I, J;
-  cta_pair(T, &I, &J);
-  if (threadIdx.x < 3) s_dc[threadIdx.x] = (float)(centers[3 * I + threadIdx.x] - centers[3 * J + threadIdx.x]);
-  for (int t = threadIdx.x; t < 2 * kB; t += kF32Threads) {
-    const int side = t / kB, k = t % kB;
-    const int g = (side ? J : I) * kB + k;
-    float4 p = pts[g];  // padded to whole tiles
-    p.w = (g < n) ? xf[g] : 0.f;
-    if (side == 0) {
-      sr[k] = p;
-    } else {
-      cq[k] = make_float4(p.x, p.x, p.y, p.y);
-      cw[k] = make_float4(p.z, p.z, p.w, p.w);
-    }
+  __shared__ float rowacc[kGroup][4][kB];
+  const int2 jm = map[blockIdx.x];
+  const int J = jm.x, g = jm.y;
+  const int I0 = kGroup * g, I1 = min(I0 + kGroup - 1, J);
+  {
+    const int t = threadIdx.x;  // 128 threads, 128 columns
+    const int gi = J * kB + t;
+    const float4 p = pts[gi];  // padded to whole tiles
+    const float w = gi < n ? xf[gi] : 0.f;
+    cq[t] = make_float4(p.x, p.x, p.y, p.y);
+    cw[t] = make_float4(p.z, p.z, w, w);
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint64_t rx[2], ry[2], rz[2], xi2[2], acc[2];
-#pragma unroll
-  for (int q = 0; q < 2; ++q) {
-    const float4 a = sr[lane + 64 * q];
-    const float4 b = sr[lane + 64 * q + 32];
-    rx[q] = f2_pack(a.x + s_dc[0], b.x + s_dc[0]);
-    ry[q] = f2_pack(a.y + s_dc[1], b.y + s_dc[1]);
-    rz[q] = f2_pack(a.z + s_dc[2], b.z + s_dc[2]);
-    xi2[q] = f2_pack(a.w, b.w);
-    acc[q] = 0ull;  // +0.0f in both halves
-  }
   float col[32];
 #pragma unroll
-  for (int b = 0; b < 32; ++b) {
-    const float4 q4 = cq[32 * warp + b];
-    const float4 w4 = cw[32 * warp + b];
-    const uint64_t qx = f2_pack(q4.x, q4.y), qy = f2_pack(q4.z, q4.w);
-    const uint64_t qz = f2_pack(w4.x, w4.y), qw = f2_pack(w4.z, w4.w);
-    uint64_t c2 = 0ull;
+  for (int b = 0; b < 32; ++b) col[b] = 0.f;
+  for (int I = I0; I <= I1; ++I) {
+    uint64_t rx[2], ry[2], rz[2], xi2[2], acc[2];
+    const bool diag = I == J;
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
-      const uint64_t dx = f2_sub(rx[q], qx);
-      uint64_t s2;
-      if (DIM == 1) {
-        s2 = f2_mul(dx, dx);
-      } else if (DIM == 2) {
-        const uint64_t dy = f2_sub(ry[q], qy);
-        s2 = f2_fma(dx, dx, f2_mul(dy, dy));
-      } else {
-        const uint64_t dy = f2_sub(ry[q], qy);
-        const uint64_t dz = f2_sub(rz[q], qz);
-        s2 = f2_fma(dx, dx, f2_fma(dy, dy, f2_mul(dz, dz)));
-      }
-      float s0, s1;
-      f2_unpack(s2, s0, s1);
-      const uint64_t e2 = f2_pack(ex2_approx(-s0), ex2_approx(-s1));
-      acc[q] = f2_fma(e2, qw, acc[q]);
-      c2 = f2_fma(e2, xi2[q], c2);
+      const int r0 = I * kB + lane + 64 * q, r1 = r0 + 32;
+      const float4 a = pts[r0], b = pts[r1];
+      const float wa = (!diag && r0 < n) ? xf[r0] : 0.f;
+      const float wb = (!diag && r1 < n) ? xf[r1] : 0.f;
+      rx[q] = f2_pack(a.x, b.x);
+      ry[q] = f2_pack(a.y, b.y);
+      rz[q] = f2_pack(a.z, b.z);
+      xi2[q] = f2_pack(wa, wb);
+      acc[q] = 0ull;  // +0.0f in both halves
     }
-    float c0, c1;
-    f2_unpack(c2, c0, c1);
-    col[b] = c0 + c1;
-  }
 #pragma unroll
-  for (int q = 0; q < 2; ++q) {
-    float a0, a1;
-    f2_unpack(acc[q], a0, a1);
-    rowbuf[warp][lane + 64 * q] = a0;
-    rowbuf[warp][lane + 64 * q + 32] = a1;
+    for (int b = 0; b < 32; ++b) {
+      const float4 q4 = cq[32 * warp + b];
+      const float4 w4 = cw[32 * warp + b];
+      const uint64_t qx = f2_pack(q4.x, q4.y), qy = f2_pack(q4.z, q4.w);
+      const uint64_t qz = f2_pack(w4.x, w4.y), qw = f2_pack(w4.z, w4.w);
+      uint64_t c2 = f2_pack(col[b], 0.f);
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const uint64_t dx = f2_sub(rx[q], qx);
+        uint64_t s2;
+        if (DIM == 1) {
+          s2 = f2_mul(dx, dx);
+        } else if (DIM == 2) {
+          const uint64_t dy = f2_sub(ry[q], qy);
+          s2 = f2_fma(dx, dx, f2_mul(dy, dy));
+        } else {
+          const uint64_t dy = f2_sub(ry[q], qy);
+          const uint64_t dz = f2_sub(rz[q], qz);
+          s2 = f2_fma(dx, dx, f2_fma(dy, dy, f2_mul(dz, dz)));
+        }
+        float s0, s1;
+        f2_unpack(s2, s0, s1);
+        const uint64_t e2 = f2_pack(ex2_approx(-s0), ex2_approx(-s1));
+        acc[q] = f2_fma(e2, qw, acc[q]);
+        c2 = f2_fma(e2, xi2[q], c2);
+      }
+      float c0, c1;
+      f2_unpack(c2, c0, c1);
+      col[b] = c0 + c1;
+    }
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      float a0, a1;
+      f2_unpack(acc[q], a0, a1);
+      rowacc[I - I0][warp][lane + 64 * q] = a0;
+      rowacc[I - I0][warp][lane + 64 * q + 32] = a1;
+    }
   }
-  if (I != J) {
-    warp_reduce_scatter32(col, lane);
-    S[((long long)J * T + I) * kB + 32 * warp + lane] = col[0];
-  }
+  warp_reduce_scatter32(col, lane);
+  Scol[((long long)J * GT + g) * kB + 32 * warp + lane] = col[0];
   __syncthreads();
-  const int r = threadIdx.x;  // 128 threads, 128 rows
-  S[((long long)I * T + J) * kB + r] = ((rowbuf[0][r] + rowbuf[1][r]) + rowbuf[2][r]) + rowbuf[3][r];
+  const int r = threadIdx.x;
+  for (int I = I0; I <= I1; ++I) {
+    const int i = I - I0;
+    Srow[((long long)I * T + J) * kB + r] = ((rowacc[i][0][r] + rowacc[i][1][r]) + rowacc[i][2][r]) + rowacc[i][3][r];
+  }
 }
 
 // xf[k] = x[perm[k]] rounded to FP32 (once per matvec, not once per tile pair)
@@ -350,23 +364,32 @@ __global__ void sym_f32_gather_kernel(int n, const int* __restrict__ perm, const
   if (k < n) xf[k] = (float)x[perm[k]];
 }
 
-// y[perm[i]] = sum over the T slots of row i + nugget x: groups of 16 slots in
-// FP32, the groups in FP64, always in slot order.
-__global__ void sym_f32_reduce_kernel(int n, int T, const float* __restrict__ S, const int* __restrict__ perm,
+// y[perm[i]] = nugget x + row slots (J >= I) + column slots (groups of the
+// column tile I): FP32 groups of 16 slots added in FP64, in a fixed order.
+__global__ void sym_f32_reduce_kernel(int n, int T, int GT, const float* __restrict__ Srow,
+                                      const float* __restrict__ Scol, const int* __restrict__ perm,
                                       const double* __restrict__ x, double nugget, double* __restrict__ y,
                                       const int* __restrict__ skip) {
   if (skip && *skip) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const int tile = i / kB, r = i % kB;
-  const float* p = S + (long long)tile * T * kB + r;
+  const int I = i / kB, r = i % kB;
   double s = 0.0;
-  for (int k0 = 0; k0 < T; k0 += 16) {
-    const int k1 = min(T, k0 + 16);
-    float g = 0.f;
+  const float* pr = Srow + (long long)I * T * kB + r;
+  for (int J0 = I; J0 < T; J0 += 16) {
+    const int J1 = min(T, J0 + 16);
+    float gsum = 0.f;
 #pragma unroll 4
-    for (int k = k0; k < k1; ++k) g += __ldcg(p + (long long)k * kB);
-    s += (double)g;
+    for (int J = J0; J < J1; ++J) gsum += __ldcg(pr + (long long)J * kB);
+    s += (double)gsum;
+  }
+  const float* pc = Scol + (long long)I * GT * kB + r;
+  const int ng = I / kGroup + 1;
+  for (int g0 = 0; g0 < ng; g0 += 16) {
+    const int g1 = min(ng, g0 + 16);
+    float gsum = 0.f;
+    for (int g = g0; g < g1; ++g) gsum += __ldcg(pc + (long long)g * kB);
+    s += (double)gsum;
   }
   const int o = perm[i];
   y[o] = fma(nugget, x[o], s);
@@ -479,44 +502,47 @@ int SymF32::init(DeviceContext* c, const GaussSystem& g, cudaStream_t s) {
   MGB_CUDA(cudaStreamSynchronize(s));
   const double scale = std::sqrt(1.4426950408889634);  // sqrt(log2 e): exp(-s) = 2^(-s log2 e)
   const std::vector<int> perm = morton_perm(h, n_, dim_);
-  // Tile centres stay zero (global coordinates): see the FP32 note at the
-  // top of the file.
-  std::vector<double> centers((size_t)3 * T_, 0.0);
-  std::vector<float4> pts((size_t)T_ * kB);
-  for (int t = 0; t < T_; ++t) {
-    const int b0 = t * kB, b1 = std::min(n_, b0 + kB);
-    for (int k = b0; k < t * kB + kB; ++k) {
-      float v[3] = {0.f, 0.f, 0.f};
-      if (k < b1)
-        for (int d = 0; d < dim_; ++d) v[d] = (float)(h[(size_t)d * n_ + perm[k]] * scale - centers[3 * t + d]);
-      pts[k] = make_float4(v[0], v[1], v[2], 0.f);
-    }
+  // global FP32 coordinates (one rounding per point: the FP32 operator is the
+  // kernel matrix of a slightly perturbed point set)
+  std::vector<float4> pts((size_t)T_ * kB, make_float4(0.f, 0.f, 0.f, 0.f));
+  for (int k = 0; k < n_; ++k) {
+    float v[3] = {0.f, 0.f, 0.f};
+    for (int d = 0; d < dim_; ++d) v[d] = (float)(h[(size_t)d * n_ + perm[k]] * scale);
+    pts[k] = make_float4(v[0], v[1], v[2], 0.f);
   }
+  GT_ = T_ / kGroup + 1;
+  std::vector<int2> map;
+  for (int J = 0; J < T_; ++J)
+    for (int g = 0; g <= J / kGroup; ++g) map.push_back(make_int2(J, g));
+  ncta_ = (long long)map.size();
+  if (ncta_ > 0x7fffffffLL) return set_error(MGB_ERR_ARG, "system too large for one grid");
+  auto up = [](size_t b) { return (b + 255) & ~size_t(255); };
   const size_t bytes_pts = sizeof(float4) * pts.size();
-  const size_t bytes_ctr = sizeof(double) * centers.size();
+  const size_t bytes_map = sizeof(int2) * map.size();
   const size_t bytes_perm = sizeof(int) * (size_t)n_;
-  MGB_TRY(pool_alloc(c, bytes_pts + bytes_ctr + bytes_perm, (void**)&pts_));
-  centers_ = reinterpret_cast<double*>(reinterpret_cast<char*>(pts_) + bytes_pts);
-  perm_ = reinterpret_cast<int*>(reinterpret_cast<char*>(centers_) + bytes_ctr);
+  MGB_TRY(pool_alloc(c, up(bytes_pts) + up(bytes_map) + up(bytes_perm), (void**)&pts_));
+  map_ = reinterpret_cast<int2*>(reinterpret_cast<char*>(pts_) + up(bytes_pts));
+  perm_ = reinterpret_cast<int*>(reinterpret_cast<char*>(map_) + up(bytes_map));
   MGB_CUDA(cudaMemcpyAsync(pts_, pts.data(), bytes_pts, cudaMemcpyHostToDevice, s));
-  MGB_CUDA(cudaMemcpyAsync(centers_, centers.data(), bytes_ctr, cudaMemcpyHostToDevice, s));
+  MGB_CUDA(cudaMemcpyAsync(map_, map.data(), bytes_map, cudaMemcpyHostToDevice, s));
   MGB_CUDA(cudaMemcpyAsync(perm_, perm.data(), bytes_perm, cudaMemcpyHostToDevice, s));
-  MGB_TRY(pool_alloc(c, sizeof(float) * ((size_t)T_ * T_ * kB + (size_t)T_ * kB), (void**)&S_));
-  xf_ = S_ + (size_t)T_ * T_ * kB;
+  const size_t nrow = (size_t)T_ * T_ * kB, ncol = (size_t)T_ * GT_ * kB;
+  MGB_TRY(pool_alloc(c, sizeof(float) * (nrow + ncol + (size_t)T_ * kB), (void**)&S_));
+  Scol_ = S_ + nrow;
+  xf_ = Scol_ + ncol;
   MGB_CUDA(cudaStreamSynchronize(s));
   return MGB_OK;
 }
 
 int SymF32::apply(const double* x, double* y, cudaStream_t s, const int* skip) {
-  const long long pairs = (long long)T_ * (T_ + 1) / 2;
-  if (pairs > 0x7fffffffLL) return set_error(MGB_ERR_ARG, "system too large for one grid");
   sym_f32_gather_kernel<<<(n_ + 255) / 256, 256, 0, s>>>(n_, perm_, x, xf_, skip);
+  const unsigned grid = (unsigned)ncta_;
   switch (dim_) {
-    case 1: sym_f32_pair_kernel<1><<<(unsigned)pairs, kF32Threads, 0, s>>>(n_, T_, pts_, centers_, xf_, S_, skip); break;
-    case 2: sym_f32_pair_kernel<2><<<(unsigned)pairs, kF32Threads, 0, s>>>(n_, T_, pts_, centers_, xf_, S_, skip); break;
-    default: sym_f32_pair_kernel<3><<<(unsigned)pairs, kF32Threads, 0, s>>>(n_, T_, pts_, centers_, xf_, S_, skip); break;
+    case 1: sym_f32_group_kernel<1><<<grid, kF32Threads, 0, s>>>(n_, T_, GT_, map_, pts_, xf_, S_, Scol_, skip); break;
+    case 2: sym_f32_group_kernel<2><<<grid, kF32Threads, 0, s>>>(n_, T_, GT_, map_, pts_, xf_, S_, Scol_, skip); break;
+    default: sym_f32_group_kernel<3><<<grid, kF32Threads, 0, s>>>(n_, T_, GT_, map_, pts_, xf_, S_, Scol_, skip); break;
   }
-  sym_f32_reduce_kernel<<<(n_ + 255) / 256, 256, 0, s>>>(n_, T_, S_, perm_, x, nugget_, y, skip);
+  sym_f32_reduce_kernel<<<(n_ + 255) / 256, 256, 0, s>>>(n_, T_, GT_, S_, Scol_, perm_, x, nugget_, y, skip);
   count_launches(3);
   MGB_CUDA(cudaGetLastError());
   return MGB_OK;

@@ -27,7 +27,8 @@ class SymF64 : public Matvec {
   double* S_ = nullptr;  // T x T x 128 slot partials
 };
 
-// FP32 + SFU on Morton-ordered, tile-centred points: the mixed-CG operator.
+// FP32 + SFU on Morton-ordered points (packed f32x2 arithmetic): the
+// default mixed-CG operator.
 class SymF32 : public Matvec {
  public:
   ~SymF32() override;
@@ -37,17 +38,19 @@ class SymF32 : public Matvec {
 
  private:
   DeviceContext* c_ = nullptr;
-  int n_ = 0, dim_ = 0, T_ = 0;
+  int n_ = 0, dim_ = 0, T_ = 0, GT_ = 0;
+  long long ncta_ = 0;
   double nugget_ = 0.0;
-  float4* pts_ = nullptr;     // T*128 points relative to their tile centre (pool block, also holds centres/perm)
-  double* centers_ = nullptr; // 3 per tile
+  float4* pts_ = nullptr;     // T*128 scaled FP32 points (pool block, also holds map_ and perm_)
+  int2* map_ = nullptr;       // CTA -> (column tile, row-tile group)
   int* perm_ = nullptr;       // sorted position -> original index
-  float* S_ = nullptr;        // T x T x 128 slot partials (pool block, also holds xf_)
+  float* S_ = nullptr;        // row slots T x T x 128 (pool block, also holds Scol_ and xf_)
+  float* Scol_ = nullptr;     // column slots T x GT x 128
   float* xf_ = nullptr;       // x gathered into sorted order, FP32
 };
 
 // FP32 + SFU with the squared distances as a BF16 tensor-core contraction
-// (gauss_tc.cu): the default mixed-CG operator.
+// (gauss_tc.cu): selectable with mgb_set_mixed_matvec.
 class SymTC : public Matvec {
  public:
   ~SymTC() override;
