@@ -72,10 +72,10 @@ __device__ __forceinline__ void pair_of(long long p, int T, int* I, int* J) {
   *J = i + (int)(p - start(i));
 }
 
-// (I, J) computed once per CTA and broadcast through shared memory.
-__device__ __forceinline__ void cta_pair(int T, int* I, int* J) {
+// (I, J) of pair p computed once per CTA and broadcast through shared memory.
+__device__ __forceinline__ void cta_pair(long long p, int T, int* I, int* J) {
   __shared__ int s_ij[2];
-  if (threadIdx.x == 0) pair_of(blockIdx.x, T, &s_ij[0], &s_ij[1]);
+  if (threadIdx.x == 0) pair_of(p, T, &s_ij[0], &s_ij[1]);
   __syncthreads();
   *I = s_ij[0];
   *J = s_ij[1];
@@ -121,17 +121,24 @@ __global__ void __launch_bounds__(kThreads) sym_f64_pair_kernel(int n, int T, co
                                                                 const double* __restrict__ c2,
                                                                 const double* __restrict__ x,
                                                                 const double* __restrict__ table_g,
-                                                                double* __restrict__ S, const int* __restrict__ skip) {
+                                                                double* __restrict__ S, long long npairs,
+                                                                const int* __restrict__ skip) {
+  // A fixed grid strides over the tile pairs, so that a launch whose skip
+  // flag is set (the mixed CG's true-residual node on most iterations)
+  // costs a few thousand CTA starts, not one per tile pair.
   if (skip && *skip) return;
-  // the exp table is dead once the entries are evaluated; the column
-  // reduction buffer (16 x 128 doubles) reuses its storage
+  // the exp table is dead once a pair's entries are evaluated; the column
+  // reduction buffer (16 x 128 doubles) reuses its storage, and the table is
+  // reloaded (from L2) for the next pair
   __shared__ double table[kExpTableSize];
   __shared__ double sp[2][DIM][kB];
   __shared__ double sxv[2][kB];
   double* colbuf = table;
   static_assert(16 * kB <= kExpTableSize, "column buffer must fit in the table storage");
+  for (long long pair = blockIdx.x; pair < npairs; pair += gridDim.x) {
   int I, J;
-  cta_pair(T, &I, &J);
+  __syncthreads();  // the previous pair's column reduction is done with colbuf
+  cta_pair(pair, T, &I, &J);
   for (int i = threadIdx.x; i < kExpTableSize; i += kThreads) table[i] = table_g[i];
   for (int t = threadIdx.x; t < 2 * kB; t += kThreads) {
     const int side = t / kB, k = t % kB;
@@ -179,6 +186,7 @@ __global__ void __launch_bounds__(kThreads) sym_f64_pair_kernel(int n, int T, co
   double* slot_row = S + ((long long)I * T + J) * kB;
   double* slot_col = diag ? nullptr : S + ((long long)J * T + I) * kB;
   store_sums<double>(acc_r, acc_c, slot_row, slot_col, colbuf, ty, tx);
+  }
 }
 
 // y_i = sum_K S[tile(i)][K][i % B] + nugget x_i
@@ -262,7 +270,16 @@ __device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
 // to the column partials (its row weights are zero there), so every
 // unordered pair of points counts once per direction.  Row sums of each row
 // tile combine the 4 warps in shared memory in warp order.
+//
+// Tile pairs whose bounding boxes are more than kFarLog2 apart (squared
+// distance in the kernel's log2 units) are not evaluated: every entry there
+// is below 2^-40, so even summed over all n columns a row loses less than
+// n * 2^-40 (6e-8 at n = 65536) -- far below the FP32 rounding of its sum and
+// the nugget.  The CTA map lists only groups with a near row tile, and a
+// 4-bit mask per CTA marks which of its row tiles are near; the slots of
+// far pairs are zeroed once and never written.
 constexpr int kGroup = 4;
+constexpr double kFarLog2 = 40.0;
 
 template <int DIM>
 __global__ void __launch_bounds__(kF32Threads) sym_f32_group_kernel(int n, int T, int GT,
@@ -277,7 +294,7 @@ __global__ void __launch_bounds__(kF32Threads) sym_f32_group_kernel(int n, int T
   __shared__ float4 cw[kB];
   __shared__ float rowacc[kGroup][4][kB];
   const int2 jm = map[blockIdx.x];
-  const int J = jm.x, g = jm.y;
+  const int J = jm.x, g = jm.y & 0xFFFF, near = jm.y >> 16;
   const int I0 = kGroup * g, I1 = min(I0 + kGroup - 1, J);
   {
     const int t = threadIdx.x;  // 128 threads, 128 columns
@@ -293,6 +310,7 @@ __global__ void __launch_bounds__(kF32Threads) sym_f32_group_kernel(int n, int T
 #pragma unroll
   for (int b = 0; b < 32; ++b) col[b] = 0.f;
   for (int I = I0; I <= I1; ++I) {
+    if (!((near >> (I - I0)) & 1)) continue;
     uint64_t rx[2], ry[2], rz[2], xi2[2], acc[2];
     const bool diag = I == J;
 #pragma unroll
@@ -352,6 +370,7 @@ __global__ void __launch_bounds__(kF32Threads) sym_f32_group_kernel(int n, int T
   const int r = threadIdx.x;
   for (int I = I0; I <= I1; ++I) {
     const int i = I - I0;
+    if (!((near >> i) & 1)) continue;
     Srow[((long long)I * T + J) * kB + r] = ((rowacc[i][0][r] + rowacc[i][1][r]) + rowacc[i][2][r]) + rowacc[i][3][r];
   }
 }
@@ -464,14 +483,14 @@ int SymF64::init(DeviceContext* c, const GaussSystem& g) {
 
 int SymF64::apply(const double* x, double* y, cudaStream_t s, const int* skip) {
   const long long pairs = (long long)T_ * (T_ + 1) / 2;
-  if (pairs > 0x7fffffffLL) return set_error(MGB_ERR_ARG, "system too large for one grid");
+  const unsigned grid = (unsigned)std::min<long long>(pairs, 4LL * c_->num_sms);
   const double* c0 = g_.coords[0];
   const double* c1 = g_.dim > 1 ? g_.coords[1] : c0;
   const double* c2 = g_.dim > 2 ? g_.coords[2] : c0;
   switch (g_.dim) {
-    case 1: sym_f64_pair_kernel<1><<<(unsigned)pairs, kThreads, 0, s>>>(g_.rows, T_, c0, c1, c2, x, c_->exp_table, S_, skip); break;
-    case 2: sym_f64_pair_kernel<2><<<(unsigned)pairs, kThreads, 0, s>>>(g_.rows, T_, c0, c1, c2, x, c_->exp_table, S_, skip); break;
-    default: sym_f64_pair_kernel<3><<<(unsigned)pairs, kThreads, 0, s>>>(g_.rows, T_, c0, c1, c2, x, c_->exp_table, S_, skip); break;
+    case 1: sym_f64_pair_kernel<1><<<grid, kThreads, 0, s>>>(g_.rows, T_, c0, c1, c2, x, c_->exp_table, S_, pairs, skip); break;
+    case 2: sym_f64_pair_kernel<2><<<grid, kThreads, 0, s>>>(g_.rows, T_, c0, c1, c2, x, c_->exp_table, S_, pairs, skip); break;
+    default: sym_f64_pair_kernel<3><<<grid, kThreads, 0, s>>>(g_.rows, T_, c0, c1, c2, x, c_->exp_table, S_, pairs, skip); break;
   }
   sym_f64_reduce_kernel<<<(g_.rows + 255) / 256, 256, 0, s>>>(g_.rows, T_, S_, x, g_.nugget, y, skip);
   count_launches(2);
@@ -511,9 +530,42 @@ int SymF32::init(DeviceContext* c, const GaussSystem& g, cudaStream_t s) {
     pts[k] = make_float4(v[0], v[1], v[2], 0.f);
   }
   GT_ = T_ / kGroup + 1;
+  // tile bounding boxes in the kernel's (log2-scaled FP32) coordinates
+  std::vector<double> blo((size_t)3 * T_, 0.0), bhi((size_t)3 * T_, 0.0);
+  for (int t = 0; t < T_; ++t) {
+    const int b0 = t * kB, b1 = std::min(n_, b0 + kB);
+    for (int d = 0; d < 3; ++d) {
+      double lo = 1e300, hi = -1e300;
+      for (int k = b0; k < b1; ++k) {
+        const float4 q = pts[k];
+        const double v = d == 0 ? q.x : (d == 1 ? q.y : q.z);
+        lo = std::min(lo, v);
+        hi = std::max(hi, v);
+      }
+      blo[3 * t + d] = lo;
+      bhi[3 * t + d] = hi;
+    }
+  }
+  auto far = [&](int a, int b) {
+    double d2 = 0.0;
+    for (int d = 0; d < 3; ++d) {
+      const double gap = std::max({0.0, blo[3 * b + d] - bhi[3 * a + d], blo[3 * a + d] - bhi[3 * b + d]});
+      d2 += gap * gap;
+    }
+    return d2 > kFarLog2;
+  };
   std::vector<int2> map;
+  pairs_near_ = 0;
   for (int J = 0; J < T_; ++J)
-    for (int g = 0; g <= J / kGroup; ++g) map.push_back(make_int2(J, g));
+    for (int g = 0; g <= J / kGroup; ++g) {
+      int near = 0;
+      for (int i = 0; i < kGroup && kGroup * g + i <= J; ++i)
+        if (!far(kGroup * g + i, J)) {
+          near |= 1 << i;
+          ++pairs_near_;
+        }
+      if (near) map.push_back(make_int2(J, g | (near << 16)));
+    }
   ncta_ = (long long)map.size();
   if (ncta_ > 0x7fffffffLL) return set_error(MGB_ERR_ARG, "system too large for one grid");
   auto up = [](size_t b) { return (b + 255) & ~size_t(255); };
@@ -530,6 +582,8 @@ int SymF32::init(DeviceContext* c, const GaussSystem& g, cudaStream_t s) {
   MGB_TRY(pool_alloc(c, sizeof(float) * (nrow + ncol + (size_t)T_ * kB), (void**)&S_));
   Scol_ = S_ + nrow;
   xf_ = Scol_ + ncol;
+  // slots of far pairs and groups are never written: zero them once
+  MGB_CUDA(cudaMemsetAsync(S_, 0, sizeof(float) * (nrow + ncol), s));
   MGB_CUDA(cudaStreamSynchronize(s));
   return MGB_OK;
 }

@@ -40,6 +40,7 @@ class SymF32 : public Matvec {
   DeviceContext* c_ = nullptr;
   int n_ = 0, dim_ = 0, T_ = 0, GT_ = 0;
   long long ncta_ = 0;
+  long long pairs_near_ = 0;  // tile pairs I <= J evaluated (the rest are below 2^-40)
   double nugget_ = 0.0;
   float4* pts_ = nullptr;     // T*128 scaled FP32 points (pool block, also holds map_ and perm_)
   int2* map_ = nullptr;       // CTA -> (column tile, row-tile group)
