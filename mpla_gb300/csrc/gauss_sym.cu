@@ -309,6 +309,7 @@ __global__ void __launch_bounds__(kF32Threads) sym_f32_group_kernel(int n, int T
   float col[32];
 #pragma unroll
   for (int b = 0; b < 32; ++b) col[b] = 0.f;
+#pragma unroll 1
   for (int I = I0; I <= I1; ++I) {
     if (!((near >> (I - I0)) & 1)) continue;
     uint64_t rx[2], ry[2], rz[2], xi2[2], acc[2];
