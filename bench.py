@@ -231,7 +231,7 @@ def bench_batched(mg, count: int, check_rows: int = 4096) -> dict:
     import oracle
     from mpla_gb300 import synth
 
-    spec = synth.batch_spec(count)
+    spec = synth.batch_spec(512)  # the first `count` systems of the 512-system workload
     systems = [synth.batch_system(spec, k) for k in range(count)]
     batch = mg.Batch(count)
     t_add0 = time.perf_counter()
@@ -255,12 +255,12 @@ def bench_batched(mg, count: int, check_rows: int = 4096) -> dict:
         statuses += [int(i.status) for i in infos]
         if g.n <= check_rows and k % 16 == 0:   # oracle check on a sample of the smaller systems
             op = oracle.GaussOp(g.scaled(), g.nugget)
-            worst_oracle = max(worst_oracle, max(oracle.true_relres(op, g.b[:, j], x[:, j])
+            worst_oracle = max(worst_oracle, max(oracle.true_relres_accurate(op, g.b[:, j], x[:, j])
                                                  for j in range(g.b.shape[1])))
     rpt, _ = batch.tuning()
     batch.close()
-    return {"workload": f"{count} Gaussian systems, n log-uniform [256,16384], d in {{2,3}}, l ~ U[0.03,0.2], "
-                        "nugget 1e-4, 1-8 N(0,1) right-hand sides, mixed precision, relres 1e-10",
+    return {"workload": f"the first {count} of 512 Gaussian systems, n log-uniform [256,16384], d in {{2,3}}, "
+                        "l ~ U[0.03,0.2], nugget 1e-4, 1-8 N(0,1) right-hand sides, mixed precision, relres 1e-10",
             "systems_per_s": count / sec, "rhs_solves_per_s": rhs_total / sec, "seconds": sec,
             "e2e_systems_per_s": count / (sec + t_add), "admission_seconds": t_add,
             "unfinished": left, "all_converged": all(s == 0 for s in statuses),
@@ -391,13 +391,13 @@ def run_ours(args, world, rank, local):
     # ---- e2e through the host-buffer entry point
     pin_pts = pts_scaled.copy()
     e2e_times = []
-    for k in range(args.e2e_steps + 1 if args.e2e_steps > 0 else 0):
+    # (the device path above has warmed the library; every e2e call is timed)
+    for k in range(args.e2e_steps):
         barrier(world)
         t0 = time.perf_counter()
         x_host, einfo = mg.cg_gauss_host(pin_pts, NUGGET, b, iter_max=args.iter_max, eps=EPS, precision=mg.PREC_MIXED)
         torch.cuda.synchronize()
-        if k > 0:
-            e2e_times.append(time.perf_counter() - t0)
+        e2e_times.append(time.perf_counter() - t0)
     e2e_sec = max_over_ranks(sum(e2e_times), world)
     e2e_value = aggregate(args.e2e_steps, e2e_sec, world) if args.e2e_steps > 0 else None
 
@@ -423,7 +423,8 @@ def run_ours(args, world, rank, local):
     sms = torch.cuda.get_device_properties(local).multi_processor_count
     sm_mhz = clocks.get("sm_mhz") or 1900.0
     entries = float(n) * n
-    mixed_rate = entries / (mixed_ms * 1e-3)
+    evaluated = float(mg.gauss_mixed_work(dp))   # exponentials one mixed matvec evaluates
+    mixed_rate = evaluated / (mixed_ms * 1e-3)
     sfu_peak = SFU_EX2_PER_CLK_SM * sms * sm_mhz * 1e6
     fp64_rate = entries / (f64_ms * 1e-3)
 
@@ -475,10 +476,13 @@ def run_ours(args, world, rank, local):
                  "iterations_assumed": iters_fp64,
                  "solves_per_s_est": fp64_solves_est,
                  "mixed_over_fp64": value / fp64_solves_est},
-        "roofline": {"bound": "sfu", "kernel": "gauss_mixed_kernel",
+        "roofline": {"bound": "sfu", "kernel": "sym_f32_group_kernel (+ gather, reduce)",
                      "achieved": mixed_rate / 1e12, "peak": sfu_peak / 1e12, "unit": "Tex2/s",
                      "frac": mixed_rate / sfu_peak, "traffic": None,
-                     "per_unit": "1 kernel entry = 1 ex2 + 6 FP32 ops; n^2 entries per launch",
+                     "per_unit": "1 evaluated kernel entry = 1 ex2 (+ ~7 FP32 issue slots); each unordered pair of "
+                                 "points evaluated once, tile pairs below 2^-40 skipped",
+                     "evaluated_per_launch": evaluated, "algorithmic_entries_per_launch": entries,
+                     "algorithmic_entries_per_s": entries / (mixed_ms * 1e-3), "matvec_ms": mixed_ms,
                      "peak_source": f"{SFU_EX2_PER_CLK_SM:.0f} ex2/clk/SM (the XU pipe peak ncu reports on GB300) "
                                     f"x {sms} SMs x {sm_mhz:.0f} MHz median SM clock"},
         "cpu_baseline": cpu,
@@ -574,10 +578,11 @@ def main(argv=None):
     p.add_argument("--no-dense", action="store_true")
     p.add_argument("--no-batched", action="store_true")
     p.add_argument("--no-serving", action="store_true")
-    p.add_argument("--batch-systems", type=int, default=512)
-    p.add_argument("--serve-rate", type=float, default=2.0)
-    p.add_argument("--serve-window", type=float, default=10.0)
-    p.add_argument("--serve-drain", type=float, default=120.0)
+    p.add_argument("--batch-systems", type=int, default=128,
+                   help="systems of the 512-system batch workload to run (a prefix: 512 runs all of it)")
+    p.add_argument("--serve-rate", type=float, default=1.0)
+    p.add_argument("--serve-window", type=float, default=5.0)
+    p.add_argument("--serve-drain", type=float, default=60.0)
     args = p.parse_args(argv)
     if args.warmup < 3:
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

@@ -161,6 +161,10 @@ int mgb_cg_gauss_host(int n, int dim, const double* coords_host, double nugget,
 #define MGB_MIXED_TENSOR 0
 #define MGB_MIXED_SIMT 1
 int mgb_set_mixed_matvec(int kind);
+/* Kernel entries (exponentials) one mixed matvec of this system evaluates:
+ * each unordered pair once, tile pairs whose entries are all below 2^-40
+ * left out (MGB_MIXED_SIMT).  The work figure of the roofline. */
+int mgb_gauss_mixed_work(int n, int dim, const double* const* coords_dev, long long* evaluated);
 int mgb_get_mixed_matvec(void);
 
 /* ------------------------------------------------------------ measurement */

@@ -47,7 +47,7 @@ C_ABI_SYMBOLS = (
     "mgb_save_vector", "mgb_load_vector",
     "mgb_batch_create", "mgb_batch_add", "mgb_batch_run", "mgb_batch_finished", "mgb_batch_result",
     "mgb_batch_tuning", "mgb_batch_destroy",
-    "mgb_set_mixed_matvec", "mgb_get_mixed_matvec",
+    "mgb_set_mixed_matvec", "mgb_get_mixed_matvec", "mgb_gauss_mixed_work",
 )
 
 
@@ -117,6 +117,7 @@ _SIGS = {
     "mgb_batch_destroy": (_I, [_P]),
     "mgb_set_mixed_matvec": (_I, [_I]),
     "mgb_get_mixed_matvec": (_I, []),
+    "mgb_gauss_mixed_work": (_I, [_I, _I, _P, C.POINTER(C.c_longlong)]),
 }
 
 
@@ -259,6 +260,13 @@ def set_mixed_matvec(kind: int) -> None:
     """Kernel of the mixed-precision matvec (MIXED_TENSOR or MIXED_SIMT) for
     matvecs and solvers set up afterwards."""
     check(lib().mgb_set_mixed_matvec(int(kind)))
+
+
+def gauss_mixed_work(pts: GaussPoints) -> int:
+    """Kernel entries one mixed matvec of this system evaluates."""
+    out = C.c_longlong()
+    check(lib().mgb_gauss_mixed_work(pts.n, pts.dim, pts.coords, C.byref(out)))
+    return out.value
 
 
 def get_mixed_matvec() -> int:

@@ -51,11 +51,15 @@ int GaussMixedMatvec::init(DeviceContext* c, const GaussSystem& g, cudaStream_t 
   if (g_mixed_kind.load() == MGB_MIXED_TENSOR) {
     SymTC* m = new SymTC();
     impl_ = m;
-    return m->init(c, g, s);
+    MGB_TRY(m->init(c, g, s));
+    evaluated_ = m->evaluated();
+    return MGB_OK;
   }
   SymF32* m = new SymF32();
   impl_ = m;
-  return m->init(c, g, s);
+  MGB_TRY(m->init(c, g, s));
+  evaluated_ = m->evaluated();
+  return MGB_OK;
 }
 
 int GaussMixedMatvec::apply(const double* x, double* y, cudaStream_t s, const int* skip) {
@@ -305,6 +309,17 @@ int mgb_time_gauss_matvec(int n, int dim, const double* const* coords, double nu
   GaussMixedMatvec A;
   MGB_TRY(A.init(c, g, s));
   return time_launches(s, reps, ms_per_launch, [&]() { return A.apply(x, y, s, nullptr); });
+}
+
+int mgb_gauss_mixed_work(int n, int dim, const double* const* coords, long long* evaluated) {
+  MGB_CTX(c);
+  if (!evaluated) return set_error(MGB_ERR_ARG, "mgb_gauss_mixed_work: null output");
+  GaussSystem g;
+  MGB_TRY(make_gauss_system(n, dim, coords, 0.0, MGB_NUGGET_DIAGONAL, &g));
+  GaussMixedMatvec A;
+  MGB_TRY(A.init(c, g, c->stream));
+  *evaluated = A.evaluated();
+  return MGB_OK;
 }
 
 int mgb_set_mixed_matvec(int kind) {

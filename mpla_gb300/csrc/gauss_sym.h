@@ -35,6 +35,8 @@ class SymF32 : public Matvec {
   int init(DeviceContext* c, const GaussSystem& g, cudaStream_t s);
   int apply(const double* x, double* y, cudaStream_t s, const int* skip) override;
   int n() const override { return n_; }
+  // kernel entries (exponentials) one apply evaluates
+  long long evaluated() const { return pairs_near_ * 128LL * 128LL; }
 
  private:
   DeviceContext* c_ = nullptr;
@@ -58,6 +60,7 @@ class SymTC : public Matvec {
   int init(DeviceContext* c, const GaussSystem& g, cudaStream_t s);
   int apply(const double* x, double* y, cudaStream_t s, const int* skip) override;
   int n() const override { return n_; }
+  long long evaluated() const { return (long long)T_ * (T_ + 1) / 2 * 128LL * 128LL; }
 
  private:
   DeviceContext* c_ = nullptr;

@@ -56,9 +56,11 @@ class GaussMixedMatvec : public Matvec {
   int init(DeviceContext* c, const GaussSystem& g, cudaStream_t s);
   int apply(const double* x, double* y, cudaStream_t s, const int* skip) override;
   int n() const override { return n_; }
+  long long evaluated() const { return evaluated_; }
 
  private:
   Matvec* impl_ = nullptr;
+  long long evaluated_ = 0;
   int n_ = 0;
 };
 
