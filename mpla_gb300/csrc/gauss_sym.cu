@@ -290,8 +290,8 @@ __global__ void __launch_bounds__(kF32Threads) sym_f32_group_kernel(int n, int T
                                                                     float* __restrict__ Scol,
                                                                     const int* __restrict__ skip) {
   if (skip && *skip) return;
-  __shared__ float4 cq[kB];
-  __shared__ float4 cw[kB];
+  __shared__ ulonglong2 cq[kB];  // {x, x} {y, y} as packed pairs
+  __shared__ ulonglong2 cw[kB];  // {z, z} {x_t, x_t}
   __shared__ float rowacc[kGroup][4][kB];
   const int2 jm = map[blockIdx.x];
   const int J = jm.x, g = jm.y & 0xFFFF, near = jm.y >> 16;
@@ -301,8 +301,8 @@ __global__ void __launch_bounds__(kF32Threads) sym_f32_group_kernel(int n, int T
     const int gi = J * kB + t;
     const float4 p = pts[gi];  // padded to whole tiles
     const float w = gi < n ? xf[gi] : 0.f;
-    cq[t] = make_float4(p.x, p.x, p.y, p.y);
-    cw[t] = make_float4(p.z, p.z, w, w);
+    cq[t] = make_ulonglong2(f2_pack(p.x, p.x), f2_pack(p.y, p.y));
+    cw[t] = make_ulonglong2(f2_pack(p.z, p.z), f2_pack(w, w));
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -328,10 +328,9 @@ __global__ void __launch_bounds__(kF32Threads) sym_f32_group_kernel(int n, int T
     }
 #pragma unroll
     for (int b = 0; b < 32; ++b) {
-      const float4 q4 = cq[32 * warp + b];
-      const float4 w4 = cw[32 * warp + b];
-      const uint64_t qx = f2_pack(q4.x, q4.y), qy = f2_pack(q4.z, q4.w);
-      const uint64_t qz = f2_pack(w4.x, w4.y), qw = f2_pack(w4.z, w4.w);
+      const ulonglong2 q2 = cq[32 * warp + b];
+      const ulonglong2 w2 = cw[32 * warp + b];
+      const uint64_t qx = q2.x, qy = q2.y, qz = w2.x, qw = w2.y;
       uint64_t c2 = f2_pack(col[b], 0.f);
 #pragma unroll
       for (int q = 0; q < 2; ++q) {
@@ -384,10 +383,12 @@ __global__ void sym_f32_gather_kernel(int n, const int* __restrict__ perm, const
   if (k < n) xf[k] = (float)x[perm[k]];
 }
 
-// y[perm[i]] = nugget x + row slots (J >= I) + column slots (groups of the
-// column tile I): FP32 groups of 16 slots added in FP64, in a fixed order.
+// y[perm[i]] = nugget x + row slots of the near column tiles J >= I (a
+// per-row-tile list) + column slots (groups of the column tile I): FP32
+// groups of 16 slots added in FP64, in a fixed order.
 __global__ void sym_f32_reduce_kernel(int n, int T, int GT, const float* __restrict__ Srow,
-                                      const float* __restrict__ Scol, const int* __restrict__ perm,
+                                      const float* __restrict__ Scol, const int* __restrict__ near_off,
+                                      const int* __restrict__ near_J, const int* __restrict__ perm,
                                       const double* __restrict__ x, double nugget, double* __restrict__ y,
                                       const int* __restrict__ skip) {
   if (skip && *skip) return;
@@ -396,11 +397,12 @@ __global__ void sym_f32_reduce_kernel(int n, int T, int GT, const float* __restr
   const int I = i / kB, r = i % kB;
   double s = 0.0;
   const float* pr = Srow + (long long)I * T * kB + r;
-  for (int J0 = I; J0 < T; J0 += 16) {
-    const int J1 = min(T, J0 + 16);
+  const int k0 = near_off[I], k1 = near_off[I + 1];
+  for (int a = k0; a < k1; a += 16) {
+    const int b = min(k1, a + 16);
     float gsum = 0.f;
-#pragma unroll 4
-    for (int J = J0; J < J1; ++J) gsum += __ldcg(pr + (long long)J * kB);
+#pragma unroll 8
+    for (int k = a; k < b; ++k) gsum += __ldcg(pr + (long long)__ldg(&near_J[k]) * kB);
     s += (double)gsum;
   }
   const float* pc = Scol + (long long)I * GT * kB + r;
@@ -408,6 +410,7 @@ __global__ void sym_f32_reduce_kernel(int n, int T, int GT, const float* __restr
   for (int g0 = 0; g0 < ng; g0 += 16) {
     const int g1 = min(ng, g0 + 16);
     float gsum = 0.f;
+#pragma unroll 8
     for (int g = g0; g < g1; ++g) gsum += __ldcg(pc + (long long)g * kB);
     s += (double)gsum;
   }
@@ -567,15 +570,28 @@ int SymF32::init(DeviceContext* c, const GaussSystem& g, cudaStream_t s) {
         }
       if (near) map.push_back(make_int2(J, g | (near << 16)));
     }
+  // per row tile I: the column tiles J >= I it is near, ascending
+  std::vector<int> near_off(T_ + 1, 0), near_J;
+  for (int I = 0; I < T_; ++I) {
+    for (int J = I; J < T_; ++J)
+      if (!far(I, J)) near_J.push_back(J);
+    near_off[I + 1] = (int)near_J.size();
+  }
   ncta_ = (long long)map.size();
   if (ncta_ > 0x7fffffffLL) return set_error(MGB_ERR_ARG, "system too large for one grid");
   auto up = [](size_t b) { return (b + 255) & ~size_t(255); };
   const size_t bytes_pts = sizeof(float4) * pts.size();
   const size_t bytes_map = sizeof(int2) * map.size();
   const size_t bytes_perm = sizeof(int) * (size_t)n_;
-  MGB_TRY(pool_alloc(c, up(bytes_pts) + up(bytes_map) + up(bytes_perm), (void**)&pts_));
+  const size_t bytes_off = sizeof(int) * near_off.size(), bytes_nj = sizeof(int) * std::max<size_t>(1, near_J.size());
+  MGB_TRY(pool_alloc(c, up(bytes_pts) + up(bytes_map) + up(bytes_perm) + up(bytes_off) + up(bytes_nj), (void**)&pts_));
   map_ = reinterpret_cast<int2*>(reinterpret_cast<char*>(pts_) + up(bytes_pts));
   perm_ = reinterpret_cast<int*>(reinterpret_cast<char*>(map_) + up(bytes_map));
+  near_off_ = reinterpret_cast<int*>(reinterpret_cast<char*>(perm_) + up(bytes_perm));
+  near_J_ = reinterpret_cast<int*>(reinterpret_cast<char*>(near_off_) + up(bytes_off));
+  MGB_CUDA(cudaMemcpyAsync(near_off_, near_off.data(), bytes_off, cudaMemcpyHostToDevice, s));
+  if (!near_J.empty())
+    MGB_CUDA(cudaMemcpyAsync(near_J_, near_J.data(), sizeof(int) * near_J.size(), cudaMemcpyHostToDevice, s));
   MGB_CUDA(cudaMemcpyAsync(pts_, pts.data(), bytes_pts, cudaMemcpyHostToDevice, s));
   MGB_CUDA(cudaMemcpyAsync(map_, map.data(), bytes_map, cudaMemcpyHostToDevice, s));
   MGB_CUDA(cudaMemcpyAsync(perm_, perm.data(), bytes_perm, cudaMemcpyHostToDevice, s));
@@ -597,7 +613,8 @@ int SymF32::apply(const double* x, double* y, cudaStream_t s, const int* skip) {
     case 2: sym_f32_group_kernel<2><<<grid, kF32Threads, 0, s>>>(n_, T_, GT_, map_, pts_, xf_, S_, Scol_, skip); break;
     default: sym_f32_group_kernel<3><<<grid, kF32Threads, 0, s>>>(n_, T_, GT_, map_, pts_, xf_, S_, Scol_, skip); break;
   }
-  sym_f32_reduce_kernel<<<(n_ + 255) / 256, 256, 0, s>>>(n_, T_, GT_, S_, Scol_, perm_, x, nugget_, y, skip);
+  sym_f32_reduce_kernel<<<(n_ + 255) / 256, 256, 0, s>>>(n_, T_, GT_, S_, Scol_, near_off_, near_J_, perm_, x,
+                                                          nugget_, y, skip);
   count_launches(3);
   MGB_CUDA(cudaGetLastError());
   return MGB_OK;

@@ -45,8 +45,10 @@ class SymF32 : public Matvec {
   long long pairs_near_ = 0;  // tile pairs I <= J evaluated (the rest are below 2^-40)
   double nugget_ = 0.0;
   float4* pts_ = nullptr;     // T*128 scaled FP32 points (pool block, also holds map_ and perm_)
-  int2* map_ = nullptr;       // CTA -> (column tile, row-tile group)
+  int2* map_ = nullptr;       // CTA -> (column tile, row-tile group | near mask << 16)
   int* perm_ = nullptr;       // sorted position -> original index
+  int* near_off_ = nullptr;   // per row tile I: offsets into near_J_
+  int* near_J_ = nullptr;     // column tiles J >= I near tile I
   float* S_ = nullptr;        // row slots T x T x 128 (pool block, also holds Scol_ and xf_)
   float* Scol_ = nullptr;     // column slots T x GT x 128
   float* xf_ = nullptr;       // x gathered into sorted order, FP32
