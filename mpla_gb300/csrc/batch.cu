@@ -288,7 +288,7 @@ __global__ void __launch_bounds__(kTile) k_bmv64(WorkQueue q, const BatchSys* __
   __shared__ double sp[DIM][kColTile];
   __shared__ double sv[kColTile * R];
   __shared__ int s_item;
-  for (int i = threadIdx.x; i < kExpTableSize; i += kTile) table[i] = table_g[i];
+  bool have_table = false;  // loaded on the first item with work (most launches have none)
   for (;;) {
     const int it = claim(q, &s_item);
     if (it >= *q.count) break;
@@ -297,6 +297,10 @@ __global__ void __launch_bounds__(kTile) k_bmv64(WorkQueue q, const BatchSys* __
     if (!sys_active(S) || S.dim != DIM || S.R != R) continue;
     if (!TRUE_RES && S.precision != MGB_PREC_FP64) continue;
     if (TRUE_RES && (S.precision != MGB_PREC_MIXED || !S.need_hi || w.chunk != 0)) continue;
+    if (!have_table) {
+      for (int i = threadIdx.x; i < kExpTableSize; i += kTile) table[i] = table_g[i];
+      have_table = true;  // the __syncthreads of the column staging below orders it
+    }
     const int n = S.n;
     const double* v = TRUE_RES ? S.x : S.d;
     const int i = w.row0 + threadIdx.x;
@@ -840,6 +844,12 @@ int BatchEngine::sync_items() {
                                s_));
     count_host_[q] = cnt;
   }
+  for (int q = 0; q < kClasses; ++q) has_mixed_[q] = has_fp64_[q] = false;
+  for (int i = 0; i < nslots_; ++i) {
+    if (!host_[i].in_use) continue;
+    const int cls = class_of(host_[i].dim, host_[i].R);
+    (host_[i].precision == MGB_PREC_MIXED ? has_mixed_ : has_fp64_)[cls] = true;
+  }
   vcount_host_ = (int)vitems_host_.size();
   if (vcount_host_)
     MGB_CUDA(cudaMemcpyAsync(vitems_, vitems_host_.data(), sizeof(VecItem) * vcount_host_, cudaMemcpyHostToDevice,
@@ -934,14 +944,13 @@ int BatchEngine::enqueue_vec(int phase) {
 
 int BatchEngine::enqueue_step() {
   for (int cls = 0; cls < kClasses; ++cls) {
-    if (!count_host_[cls]) continue;
-    MGB_TRY(enqueue_mv32(cls, rpt_[cls] ? rpt_[cls] : 2));
-    MGB_TRY(enqueue_mv64(cls, Q_MV64));
+    if (has_mixed_[cls]) MGB_TRY(enqueue_mv32(cls, rpt_[cls] ? rpt_[cls] : 2));
+    if (has_fp64_[cls]) MGB_TRY(enqueue_mv64(cls, Q_MV64));
   }
   MGB_TRY(enqueue_vec(0));
   MGB_TRY(enqueue_vec(1));
   for (int cls = 0; cls < kClasses; ++cls)
-    if (count_host_[cls]) MGB_TRY(enqueue_mv64(cls, Q_MV64_TRUE));
+    if (has_mixed_[cls]) MGB_TRY(enqueue_mv64(cls, Q_MV64_TRUE));
   MGB_TRY(enqueue_vec(2));
   MGB_TRY(enqueue_vec(3));
   k_bcount<<<1, 256, 0, s_>>>(dev_sys_, nslots_, counters_ + kOffActive);
@@ -1000,8 +1009,8 @@ int BatchEngine::run_steps(int steps, int* active_out) {
   // (re)capture when the set of non-empty classes, the slot range or a
   // tuning choice changed
   unsigned int sig = 0;
-  for (int q = 0; q < kClasses; ++q) sig |= (count_host_[q] ? 1u : 0u) << q;
-  sig |= (unsigned)nslots_ << 8;
+  for (int q = 0; q < kClasses; ++q) sig |= (has_mixed_[q] ? 1u : 0u) << q | (has_fp64_[q] ? 1u : 0u) << (q + 8);
+  sig = sig * 31u + (unsigned)nslots_;
   for (int q = 0; q < kClasses; ++q) sig = sig * 31u + (unsigned)rpt_[q];
   if (!graph_exec_ || sig != graph_sig_) {
     if (graph_exec_) cudaGraphExecDestroy(graph_exec_);

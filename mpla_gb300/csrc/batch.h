@@ -104,6 +104,8 @@ class BatchEngine {
   BatchItem* items_[kClasses] = {};
   std::vector<BatchItem> items_host_[kClasses];
   int count_host_[kClasses] = {};
+  bool has_mixed_[kClasses] = {};  // classes holding mixed / FP64 systems
+  bool has_fp64_[kClasses] = {};
   VecItem* vitems_ = nullptr;
   std::vector<VecItem> vitems_host_;
   int vcount_host_ = 0;
