@@ -8,6 +8,7 @@ that ends by itself (a few hundred MB on the device at most):
   python -m mpla_gb300.profile_cases gauss_mixed # FP32/SFU Gaussian matvec, n = 65536, d = 2
   python -m mpla_gb300.profile_cases mixed_cg    # 300 mixed-CG iterations, n = 16384, d = 2
   python -m mpla_gb300.profile_cases batch       # 100 steps of a 24-system batch (n <= 4096)
+  python -m mpla_gb300.profile_cases mixed_c3    # full mixed solve, n = 131072, d = 3, l = 0.08
   python -m mpla_gb300.profile_cases all
 
 Prints the CUDA-event time per launch of each case.
@@ -77,13 +78,35 @@ def case_batch(steps=100):
     batch.close()
 
 
+def case_mixed_c3():
+    """The mixed-precision configuration: n = 131072 points U[0,1]^3, l = 0.08,
+    nugget 1e-4, b = sin(2 pi x1) cos(2 pi x2), solved to relres 1e-10."""
+    import time
+
+    n = 131072
+    prob = synth.config_gauss_mixed(0)
+    dp = mg.GaussPoints(prob.scaled())
+    b = mg.DeviceArray.from_numpy(prob.b)
+    x = mg.DeviceArray(n)
+    x.zero()
+    mv_ms = mg.time_gauss_matvec(dp, 1e-4, mg.PREC_MIXED, b.ptr, x.ptr, reps=5)
+    evaluated = mg.gauss_mixed_work(dp)
+    x.zero()
+    t0 = time.perf_counter()
+    info = mg.cg_gauss(dp, 1e-4, b.ptr, x.ptr, iter_max=200000, eps=1e-10, precision=mg.PREC_MIXED)
+    sec = time.perf_counter() - t0
+    print(f"mixed_c3 n={n} d=3: matvec {mv_ms:.3f} ms ({evaluated} evaluated entries), {info.iterations} iterations, "
+          f"{info.fp64_matvecs} FP64 true residuals, {sec:.2f} s, true relres {info.true_relres:.3e}, "
+          f"status {info.status}")
+
+
 CASES = {"dgemv": case_dgemv, "gauss_f64": case_gauss_f64, "gauss_mixed": case_gauss_mixed,
-         "mixed_cg": case_mixed_cg, "batch": case_batch}
+         "mixed_cg": case_mixed_cg, "batch": case_batch, "mixed_c3": case_mixed_c3}
 
 
 def main(argv):
     mg.init(0)
-    names = list(CASES) if (not argv or argv[0] == "all") else argv
+    names = [k for k in CASES if k != "mixed_c3"] if (not argv or argv[0] == "all") else argv
     for name in names:
         CASES[name]()
     mg.synchronize()
