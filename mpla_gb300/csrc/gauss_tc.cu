@@ -30,6 +30,7 @@
 // K_ii = 1), so the operator is exactly symmetric.  Row and column sums go
 // to per-pair slots reduced in a fixed order: the matvec is reproducible.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -510,12 +511,14 @@ int SymTC::init(DeviceContext* c, const GaussSystem& g, cudaStream_t s) {
   MGB_TRY(pool_alloc(c, sizeof(float) * (nrow + ncol + npad), (void**)&S_));
   Scol_ = S_ + nrow;
   xf_ = Scol_ + ncol;
-  static bool attr_set[64] = {false};
-  if (c->device >= 0 && c->device < 64 && !attr_set[c->device]) {
+  // the kernels' shared-memory limit, once per device (a function attribute
+  // of the current device; cheap and idempotent, so a race only repeats it)
+  static std::atomic<bool> attr_set[64];
+  if (c->device >= 0 && c->device < 64 && !attr_set[c->device].load()) {
     MGB_CUDA(cudaFuncSetAttribute(sym_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmRequest));
     MGB_CUDA(cudaFuncSetAttribute(sym_tc_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmRequest));
     MGB_CUDA(cudaFuncSetAttribute(sym_tc_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmRequest));
-    attr_set[c->device] = true;
+    attr_set[c->device].store(true);
   }
   MGB_CUDA(cudaStreamSynchronize(s));
   return MGB_OK;

@@ -135,3 +135,23 @@ def test_mixed_matvec_is_bit_reproducible(gpu, mixed_kind):
         gpu.synchronize()
         outs.append(dy.numpy())
     assert np.array_equal(outs[0], outs[1])
+
+
+def test_mixed_matvec_far_pairs_left_out(gpu, orc, mixed_kind):
+    # a short length scale: most tile pairs are farther apart than the 2^-40
+    # threshold and are not evaluated by the FP32-difference kernel; the
+    # product must meet the same bar, and its work figure must show the cut
+    n, dim, ell = 8192, 2, 0.01
+    pts = scaled_points(n, dim, ell, seed=9)
+    x = np.random.default_rng(9).standard_normal(n)
+    dp = gpu.GaussPoints(pts)
+    dx, dy = gpu.DeviceArray.from_numpy(x), gpu.DeviceArray(n)
+    gpu.gauss_matvec_mixed(dp, 1e-4, dx.ptr, dy.ptr)
+    op = orc.GaussOp(pts, 1e-4)
+    assert rel_err(dy.numpy(), op.matvec(x), abs_matvec(op, x)) <= 2e-5
+    evaluated = gpu.gauss_mixed_work(dp)
+    half = (n // 128) * (n // 128 + 1) // 2 * 128 * 128
+    if mixed_kind == gpu.MIXED_SIMT:
+        assert evaluated < half // 4
+    else:
+        assert evaluated == half
