@@ -84,6 +84,17 @@ struct DeviceContext {
   // split-K partials for dgemv / matvecs (grown on demand, never shrunk)
   double* split_partials = nullptr;
   size_t split_partials_count = 0;
+  // instantiated iteration graphs of earlier solves, keyed by every value
+  // their launches bake in (least recently used evicted)
+  struct CachedGraph {
+    std::vector<uintptr_t> key;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long long kernels = 0;
+    long long last_use = 0;
+  };
+  std::vector<CachedGraph> graph_cache;
+  long long graph_clock = 0;
 };
 
 // Context of the current device (created on first use).
@@ -139,6 +150,13 @@ struct Matvec {
   // True when apply() only enqueues device work (so it can be graph-captured).
   virtual bool capturable() const { return true; }
   virtual int n() const = 0;
+  // Appends every value apply() bakes into captured launches (pointers,
+  // sizes) and returns true, when a captured iteration graph may be reused
+  // by a later solve with the same values; false: never reuse.
+  virtual bool graph_key(std::vector<uintptr_t>* key) const {
+    (void)key;
+    return false;
+  }
 };
 
 // Krylov drivers (solvers.cu).

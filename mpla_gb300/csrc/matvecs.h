@@ -24,6 +24,11 @@ class DenseMatvec : public Matvec {
   DenseMatvec(DeviceContext* c, int n, const double* A, int lda) : c_(c), n_(n), A_(A), lda_(lda) {}
   int apply(const double* x, double* y, cudaStream_t s, const int* skip) override;
   int n() const override { return n_; }
+  bool graph_key(std::vector<uintptr_t>* key) const override {
+    key->insert(key->end(), {1u, (uintptr_t)n_, (uintptr_t)A_, (uintptr_t)lda_, (uintptr_t)c_->split_partials,
+                             (uintptr_t)c_->split_partials_count, (uintptr_t)c_->tickets, (uintptr_t)c_->dev_error});
+    return true;
+  }
 
  private:
   DeviceContext* c_;

@@ -158,6 +158,10 @@ int check_device_error(DeviceContext* c, cudaStream_t s) {
 
 static void destroy_context(DeviceContext* c) {
   cudaStreamSynchronize(c->stream);
+  for (auto& g : c->graph_cache) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    if (g.graph) cudaGraphDestroy(g.graph);
+  }
   for (auto& kv : c->free_blocks)
     for (void* p : kv.second) cudaFree(p);
   for (auto& kv : c->live_blocks) cudaFree(kv.first);

@@ -458,10 +458,45 @@ int finish_info(DeviceContext* c, SolverState* st_dev, mgb_solve_info* info, dou
 
 // Generic chunked loop: runs `one_iter` (which enqueues one iteration) until
 // the device stop flag is set.  Graph-captured when possible.
+// The kChunk-iteration graph of an earlier solve whose launches baked in the
+// same values (`key`), or null.
+DeviceContext::CachedGraph* cached_graph(DeviceContext* c, const std::vector<uintptr_t>& key) {
+  for (auto& g : c->graph_cache)
+    if (g.key == key) {
+      g.last_use = ++c->graph_clock;
+      return &g;
+    }
+  return nullptr;
+}
+
+// Keep an instantiated graph for later solves (at most 8, least recently
+// used evicted); takes ownership of g's graph and exec.
+void keep_graph(DeviceContext* c, const std::vector<uintptr_t>& key, GraphHolder* g) {
+  if (c->graph_cache.size() >= 8) {
+    auto lru = c->graph_cache.begin();
+    for (auto it = c->graph_cache.begin(); it != c->graph_cache.end(); ++it)
+      if (it->last_use < lru->last_use) lru = it;
+    cudaGraphExecDestroy(lru->exec);
+    cudaGraphDestroy(lru->graph);
+    c->graph_cache.erase(lru);
+  }
+  DeviceContext::CachedGraph e;
+  e.key = key;
+  e.graph = g->graph;
+  e.exec = g->exec;
+  e.kernels = g->kernels;
+  e.last_use = ++c->graph_clock;
+  c->graph_cache.push_back(e);
+  g->graph = nullptr;
+  g->exec = nullptr;
+}
+
 template <class OneIter, class AfterChunk>
 int run_loop(DeviceContext* c, Matvec& A, SolverState* st_dev, const SolveOptions& o, double* hist_dev,
-             std::vector<double>& hist_host, cudaStream_t s, OneIter one_iter, AfterChunk after_chunk) {
+             std::vector<double>& hist_host, cudaStream_t s, OneIter one_iter, AfterChunk after_chunk,
+             const std::vector<uintptr_t>* cache_key = nullptr) {
   GraphHolder g_chunk, g_one;
+  DeviceContext::CachedGraph* cached = cache_key ? cached_graph(c, *cache_key) : nullptr;
   const bool graphs = A.capturable();
   int k_printed = 0;
   for (;;) {
@@ -488,9 +523,15 @@ int run_loop(DeviceContext* c, Matvec& A, SolverState* st_dev, const SolveOption
       continue;
     }
     if (todo == kChunk) {
-      if (!g_chunk.exec) MGB_TRY(capture_iterations(s, kChunk, one_iter, &g_chunk));
-      MGB_CUDA(cudaGraphLaunch(g_chunk.exec, s));
-      count_launches(g_chunk.kernels);
+      if (!cached && !g_chunk.exec) {
+        MGB_TRY(capture_iterations(s, kChunk, one_iter, &g_chunk));
+        if (cache_key) {
+          keep_graph(c, *cache_key, &g_chunk);
+          cached = cached_graph(c, *cache_key);
+        }
+      }
+      MGB_CUDA(cudaGraphLaunch(cached ? cached->exec : g_chunk.exec, s));
+      count_launches(cached ? cached->kernels : g_chunk.kernels);
     } else {
       if (!g_one.exec) MGB_TRY(capture_iterations(s, 1, one_iter, &g_one));
       for (int i = 0; i < todo; ++i) {
@@ -559,7 +600,14 @@ int solve_cg(DeviceContext* c, Matvec& A, const double* b, double* x, const Solv
     }
     return MGB_OK;
   };
-  MGB_TRY(run_loop(c, A, st, o, hist, hist_host, s, one_iter, after_chunk));
+  // plain solves reuse the iteration graph of an earlier solve that baked in
+  // the same pointers and sizes (repeated solves get the same pool blocks)
+  std::vector<uintptr_t> key;
+  const bool reuse = !o.print_every && !o.checkpoint_every && !o.restart && A.graph_key(&key);
+  if (reuse)
+    key.insert(key.end(), {2u, (uintptr_t)n, (uintptr_t)x, (uintptr_t)r, (uintptr_t)d, (uintptr_t)z, (uintptr_t)st,
+                           (uintptr_t)s, (uintptr_t)c->partials, (uintptr_t)c->tickets, (uintptr_t)o.stop_rule});
+  MGB_TRY(run_loop(c, A, st, o, hist, hist_host, s, one_iter, after_chunk, reuse ? &key : nullptr));
   int status = finish_info(c, st, info, t0, s);
   if (info) {
     info->fp64_matvecs = info->iterations + 1;

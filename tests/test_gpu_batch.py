@@ -140,3 +140,34 @@ def test_admission_refuses_when_memory_is_short(gpu):
         batch.add(pts, 1e-4, np.zeros((256, 9)))
     assert e.value.status == gpu.MGB_ERR_ARG
     batch.close()
+
+
+def test_batch_edge_cases(gpu, orc):
+    batch = gpu.Batch(8)
+    # one point: K = 1 + nugget, x = b / (1 + nugget)
+    p1 = np.array([[0.3], [0.7]])
+    b1 = np.array([[2.0, -1.0]])
+    h1 = batch.add(p1, 1e-4, b1, precision=gpu.PREC_MIXED)
+    # 129 points (one full tile and one row), 8 right-hand sides, one of them 0
+    p2, b2 = make_system(31, 129, 3, 0.1, 8)
+    b2[:, 5] = 0.0
+    h2 = batch.add(p2, 1e-4, b2, precision=gpu.PREC_MIXED)
+    # iteration cap of 1: nothing runs, reported as not converged
+    p3, b3 = make_system(32, 200, 2, 0.1, 1)
+    h3 = batch.add(p3, 1e-4, b3, precision=gpu.PREC_FP64, iter_max=1)
+    assert batch.run() == 0
+    x1, i1 = batch.result(h1, 1, 2)
+    assert all(i.status == 0 for i in i1)
+    assert np.allclose(x1[0], b1[0] / (1.0 + 1e-4), rtol=1e-12)
+    x2, i2 = batch.result(h2, 129, 8)
+    assert i2[5].status == 0 and i2[5].iterations == 0 and np.all(x2[:, 5] == 0.0)
+    b2_nz = [k for k in range(8) if k != 5]
+    check_solution(orc, p2, b2[:, b2_nz], x2[:, b2_nz], [i2[k] for k in b2_nz], 1)
+    _, i3 = batch.result(h3, 200, 1)
+    assert i3[0].status == gpu.MGB_ERR_NOTCONV
+    for bad in [dict(points=np.zeros((4, 10)), b=np.ones(10)),       # dim 4
+                dict(points=np.zeros((2, 10)), b=np.ones((10, 0)))]:  # no right-hand side
+        with pytest.raises(gpu.MplaError) as e:
+            batch.add(bad["points"], 1e-4, bad["b"])
+        assert e.value.status == gpu.MGB_ERR_ARG
+    batch.close()
