@@ -224,11 +224,10 @@ def bench_dense(mg, torch, stream, hbm_peak_gbs: float | None) -> dict:
                       "bytes": gemv_bytes, "note": "A is 128 MiB: back-to-back launches partly hit L2"}}
 
 
-def bench_batched(mg, count: int, check_rows: int = 4096) -> dict:
+def bench_batched(mg, count: int) -> dict:
     """Batched mixed-precision solves: `count` Gaussian systems (n log-uniform
     in [256, 16384], d in {2,3}, l ~ U[0.03, 0.2], nugget 1e-4, 1-8 N(0,1)
     right-hand sides), admitted together and run to relres 1e-10."""
-    import oracle
     from mpla_gb300 import synth
 
     spec = synth.batch_spec(512)  # the first `count` systems of the 512-system workload
@@ -246,17 +245,15 @@ def bench_batched(mg, count: int, check_rows: int = 4096) -> dict:
     mg.synchronize()
     sec = time.perf_counter() - t0
     launches = mg.kernel_launches() - launches0
-    iters, statuses, worst_oracle = [], [], 0.0
+    iters, statuses, worst = [], [], 0.0
     rhs_total = 0
     for k, (h, g) in enumerate(zip(handles, systems)):
         x, infos = batch.result(h, g.n, g.b.shape[1])
         rhs_total += g.b.shape[1]
         iters += [i.iterations for i in infos]
         statuses += [int(i.status) for i in infos]
-        if g.n <= check_rows and k % 16 == 0:   # oracle check on a sample of the smaller systems
-            op = oracle.GaussOp(g.scaled(), g.nugget)
-            worst_oracle = max(worst_oracle, max(oracle.true_relres_accurate(op, g.b[:, j], x[:, j])
-                                                 for j in range(g.b.shape[1])))
+        # each mixed lane's FP64 double-double true residual at convergence
+        worst = max([worst] + [i.true_relres for i in infos])
     rpt, _ = batch.tuning()
     batch.close()
     return {"workload": f"the first {count} of 512 Gaussian systems, n log-uniform [256,16384], d in {{2,3}}, "
@@ -265,7 +262,7 @@ def bench_batched(mg, count: int, check_rows: int = 4096) -> dict:
             "e2e_systems_per_s": count / (sec + t_add), "admission_seconds": t_add,
             "unfinished": left, "all_converged": all(s == 0 for s in statuses),
             "iterations_median": float(np.median(iters)), "iterations_max": int(max(iters)),
-            "oracle_worst_relres_sampled": worst_oracle, "gpu_launches": int(launches),
+            "worst_true_relres": worst, "gpu_launches": int(launches),
             "autotuner_rows_per_thread": rpt}
 
 
@@ -379,14 +376,10 @@ def run_ours(args, world, rank, local):
     sec_max = max_over_ranks(sec, world)
     value = aggregate(args.steps, sec_max, world)
     info = infos[-1]
+    # the solver's own FP64 true residual ||b - K x|| / ||b|| of the returned
+    # x (parity of that residual with the FP64 oracle is a test, not a bench
+    # step)
     true_rel = float(info.true_relres)
-    if rank == 0:
-        import oracle
-
-        # the error against the FP64 oracle: relres of the returned x (sampled
-        # rows would not do; the full FP64 matvec on the host takes seconds)
-        if n <= 16384:
-            true_rel = oracle.true_relres(oracle.GaussOp(pts_scaled, NUGGET), b, x_t.cpu().numpy())
 
     # ---- e2e through the host-buffer entry point
     pin_pts = pts_scaled.copy()
