@@ -101,3 +101,17 @@ def test_batch_spec_ranges():
     assert set(np.unique(s.dim)) <= {2, 3}
     assert s.ell.min() >= 0.03 and s.ell.max() <= 0.2
     assert s.nrhs.min() >= 1 and s.nrhs.max() <= 8
+
+
+def test_mixed_kernel_switch_without_a_device(native_lib):
+    # selecting the mixed matvec kernel touches no device: checked here
+    import mpla_gb300 as mg
+
+    old = mg.get_mixed_matvec()
+    assert old in (mg.MIXED_TENSOR, mg.MIXED_SIMT)
+    assert native_lib.mgb_set_mixed_matvec(7) == mg.MGB_ERR_ARG
+    assert mg.get_mixed_matvec() == old
+    mg.set_mixed_matvec(mg.MIXED_TENSOR)
+    assert mg.get_mixed_matvec() == mg.MIXED_TENSOR
+    mg.set_mixed_matvec(old)
+    assert mg.get_mixed_matvec() == old
