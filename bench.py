@@ -256,6 +256,25 @@ def bench_batched(mg, count: int) -> dict:
         worst = max([worst] + [i.true_relres for i in infos])
     rpt, _ = batch.tuning()
     batch.close()
+
+    # plain FP64 against mixed on the same systems: a full FP64 batch would
+    # run for tens of minutes on GB300's FP64 pipe, so both precisions are
+    # timed over the same 16 steps at full occupancy (after an 8-step warm-up
+    # that also tunes and captures); FP64 CG needs ~0.75x the iterations
+    def ms_per_step(precision: int, steps: int = 16) -> float:
+        bt = mg.Batch(count)
+        for g in systems:
+            bt.add(g.scaled(), g.nugget, g.b, precision=precision, eps=EPS, iter_max=300000)
+        bt.run(max_steps=8)
+        mg.synchronize()
+        t = time.perf_counter()
+        bt.run(max_steps=steps)
+        mg.synchronize()
+        dt = (time.perf_counter() - t) / steps
+        bt.close()
+        return dt * 1e3
+
+    fp64_step, mixed_step = ms_per_step(mg.PREC_FP64), ms_per_step(mg.PREC_MIXED)
     return {"workload": f"the first {count} of 512 Gaussian systems, n log-uniform [256,16384], d in {{2,3}}, "
                         "l ~ U[0.03,0.2], nugget 1e-4, 1-8 N(0,1) right-hand sides, mixed precision, relres 1e-10",
             "systems_per_s": count / sec, "rhs_solves_per_s": rhs_total / sec, "seconds": sec,
@@ -263,6 +282,8 @@ def bench_batched(mg, count: int) -> dict:
             "unfinished": left, "all_converged": all(s == 0 for s in statuses),
             "iterations_median": float(np.median(iters)), "iterations_max": int(max(iters)),
             "worst_true_relres": worst, "gpu_launches": int(launches),
+            "fp64_ms_per_step": fp64_step, "mixed_ms_per_step": mixed_step,
+            "mixed_over_fp64_per_step": fp64_step / mixed_step,
             "autotuner_rows_per_thread": rpt}
 
 
