@@ -33,10 +33,10 @@
 // live in device memory, so systems are added and retired between replays
 // (the serving loop) without re-capturing.
 //
-// Mixed precision.  K~ is the FP32 operator: coordinates are carried as an
-// FP32 pair (hi, lo) so that a coordinate difference is accurate to FP32
-// rounding of the difference itself (not of the coordinates), and K~ is
-// exactly symmetric.  The outer iteration is iterative refinement with
+// Mixed precision.  K~ is the FP32 operator: every scaled coordinate is
+// rounded once to FP32, so K~ is the Gaussian kernel matrix of a slightly
+// perturbed point set (positive definite again, exactly symmetric) up to the
+// rounding of each entry.  The outer iteration is iterative refinement with
 // reliable residual replacement: when the recursive residual has fallen
 // 100x since the last FP64 true residual, when it claims convergence, or at
 // the iteration cap, r = b - K x in FP64 replaces it and the search
@@ -116,11 +116,6 @@ __device__ __forceinline__ uint64_t f2_pack(float lo, float hi) {
 __device__ __forceinline__ void f2_unpack(uint64_t v, float& lo, float& hi) {
   asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
 }
-__device__ __forceinline__ uint64_t f2_add(uint64_t a, uint64_t b) {
-  uint64_t r;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
 __device__ __forceinline__ uint64_t f2_sub(uint64_t a, uint64_t b) {
   uint64_t r;
   asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
@@ -138,18 +133,15 @@ __device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
 }
 
 // Partial (K~ d) over one column chunk for the R lanes of mixed systems of one
-// class, into P[chunk].  A thread owns RPT rows (RPT/2 packed pairs: rows r and r + 128 of a pair of
-// tiles); column values are staged in shared memory twice over so that one
-// load gives a packed operand.  Coordinate differences are
-// fl(fl(hi_i - hi_j) + fl(lo_i - lo_j)): exact-symmetric and accurate to the
-// rounding of the difference itself.  Per 128-column tile the products are
-// summed in FP32, and the tile sums in FP64.
+// class, into P[chunk].  A thread owns RPT rows (RPT/2 packed pairs: rows r
+// and r + 128 of a pair of tiles); column values are staged in shared memory
+// twice over so that one load gives a packed operand.  Per 128-column tile
+// the products are summed in FP32, and the tile sums in FP64.
 template <int DIM, int R, int RPT>
 __global__ void __launch_bounds__(kTile) k_bmv32(WorkQueue q, const BatchSys* __restrict__ sys) {
   constexpr int NP = RPT / 2;  // packed row pairs per thread
-  __shared__ float4 shx[kColTile];  // {hx, hx, hy, hy}
-  __shared__ float4 slx[kColTile];  // {lx, lx, ly, ly}
-  __shared__ float4 sz[kColTile];   // {hz, hz, lz, lz}
+  __shared__ float4 shx[kColTile];  // {x, x, y, y}
+  __shared__ float2 sz[kColTile];   // {z, z}
   __shared__ float2 sd[kColTile * R];
   __shared__ int s_item;
   for (;;) {
@@ -162,20 +154,16 @@ __global__ void __launch_bounds__(kTile) k_bmv32(WorkQueue q, const BatchSys* __
     // RPT consecutive tiles and takes only every RPT-th item
     if ((w.row0 / kTile) % RPT != 0) continue;
     const int n = S.n;
-    uint64_t hx[NP], hy[NP], hz[NP], lx[NP], ly[NP], lz[NP];
+    uint64_t hx[NP], hy[NP], hz[NP];
     int row[RPT];
 #pragma unroll
     for (int p = 0; p < NP; ++p) {
       row[2 * p] = w.row0 + threadIdx.x + kTile * (2 * p);
       row[2 * p + 1] = row[2 * p] + kTile;
       const float4 h0 = S.pts_hi[min(row[2 * p], n - 1)], h1 = S.pts_hi[min(row[2 * p + 1], n - 1)];
-      const float4 l0 = S.pts_lo[min(row[2 * p], n - 1)], l1 = S.pts_lo[min(row[2 * p + 1], n - 1)];
       hx[p] = f2_pack(h0.x, h1.x);
       hy[p] = f2_pack(h0.y, h1.y);
       hz[p] = f2_pack(h0.z, h1.z);
-      lx[p] = f2_pack(l0.x, l1.x);
-      ly[p] = f2_pack(l0.y, l1.y);
-      lz[p] = f2_pack(l0.z, l1.z);
     }
     double acc[RPT][R];
 #pragma unroll
@@ -189,10 +177,8 @@ __global__ void __launch_bounds__(kTile) k_bmv32(WorkQueue q, const BatchSys* __
       for (int t = threadIdx.x; t < kColTile; t += kTile) {
         const bool in = t < nj;
         const float4 h = in ? S.pts_hi[j0 + t] : make_float4(0.f, 0.f, 0.f, 0.f);
-        const float4 l = in ? S.pts_lo[j0 + t] : make_float4(0.f, 0.f, 0.f, 0.f);
         shx[t] = make_float4(h.x, h.x, h.y, h.y);
-        slx[t] = make_float4(l.x, l.x, l.y, l.y);
-        sz[t] = make_float4(h.z, h.z, l.z, l.z);
+        sz[t] = make_float2(h.z, h.z);
 #pragma unroll
         for (int k = 0; k < R; ++k) {
           const float v = in ? S.d32[(long long)(j0 + t) * R + k] : 0.f;
@@ -207,14 +193,12 @@ __global__ void __launch_bounds__(kTile) k_bmv32(WorkQueue q, const BatchSys* __
         for (int k = 0; k < R; ++k) part[p][k] = 0ull;
 #pragma unroll 2
       for (int t = 0; t < nj; ++t) {
-        const float4 H = shx[t], L = slx[t];
+        const float4 H = shx[t];
         const uint64_t qhx = f2_pack(H.x, H.y), qhy = f2_pack(H.z, H.w);
-        const uint64_t qlx = f2_pack(L.x, L.y), qly = f2_pack(L.z, L.w);
-        uint64_t qhz = 0ull, qlz = 0ull;
+        uint64_t qhz = 0ull;
         if (DIM == 3) {
-          const float4 Z = sz[t];
+          const float2 Z = sz[t];
           qhz = f2_pack(Z.x, Z.y);
-          qlz = f2_pack(Z.z, Z.w);
         }
         uint64_t dv[R];
 #pragma unroll
@@ -224,13 +208,13 @@ __global__ void __launch_bounds__(kTile) k_bmv32(WorkQueue q, const BatchSys* __
         }
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
-          const uint64_t dx = f2_add(f2_sub(hx[p], qhx), f2_sub(lx[p], qlx));
-          const uint64_t dy = f2_add(f2_sub(hy[p], qhy), f2_sub(ly[p], qly));
+          const uint64_t dx = f2_sub(hx[p], qhx);
+          const uint64_t dy = f2_sub(hy[p], qhy);
           uint64_t s2;
           if (DIM == 2) {
             s2 = f2_fma(dx, dx, f2_mul(dy, dy));
           } else {
-            const uint64_t dz = f2_add(f2_sub(hz[p], qhz), f2_sub(lz[p], qlz));
+            const uint64_t dz = f2_sub(hz[p], qhz);
             s2 = f2_fma(dx, dx, f2_fma(dy, dy, f2_mul(dz, dz)));
           }
           float s0, s1;
@@ -714,7 +698,7 @@ size_t BatchEngine::bytes_needed(int n, int dim, int nrhs, int precision) {
   b += sizeof(double) * nv * chunks_of(n) + pad;        // matvec partials
   b += sizeof(double) * 8 * vec_items_of(n) + pad;      // vector-phase partials
   b += sizeof(unsigned int) + pad;                      // ticket
-  if (precision == MGB_PREC_MIXED) b += 2 * (sizeof(float4) * (size_t)n + pad) + sizeof(float) * nv + pad;
+  if (precision == MGB_PREC_MIXED) b += (sizeof(float4) * (size_t)n + pad) + sizeof(float) * nv + pad;
   return b;
 }
 
@@ -778,33 +762,25 @@ int BatchEngine::add(int n, int dim, const double* coords_host, double nugget, i
   S.lanes = (BatchLane*)take(sizeof(BatchLane) * 8);
   if (precision == MGB_PREC_MIXED) {
     S.pts_hi = (const float4*)take(sizeof(float4) * (size_t)n);
-    S.pts_lo = (const float4*)take(sizeof(float4) * (size_t)n);
     S.d32 = (float*)take(sizeof(float) * nv);
   }
-  // host staging: interleave b; split the scaled coordinates into FP32 pairs
+  // host staging: interleave b; scaled coordinates rounded once to FP32
   std::vector<double> bh(nv, 0.0);
   for (int k = 0; k < nrhs; ++k)
     for (int i = 0; i < n; ++i) bh[(size_t)i * R + k] = b_host[(size_t)k * n + i];
   MGB_CUDA(cudaMemcpyAsync(S.b, bh.data(), sizeof(double) * nv, cudaMemcpyHostToDevice, s_));
   MGB_CUDA(cudaMemcpyAsync((void*)S.pts64, coords_host, sizeof(double) * (size_t)n * dim, cudaMemcpyHostToDevice,
                            s_));
-  std::vector<float4> ph, pl;
+  std::vector<float4> ph;
   if (precision == MGB_PREC_MIXED) {
     ph.resize(n);
-    pl.resize(n);
     const double sc = std::sqrt(1.4426950408889634);  // exp(-s) = 2^(-s log2 e)
     for (int i = 0; i < n; ++i) {
-      float h[3] = {0.f, 0.f, 0.f}, l[3] = {0.f, 0.f, 0.f};
-      for (int d = 0; d < dim; ++d) {
-        const double v = coords_host[(size_t)d * n + i] * sc;
-        h[d] = (float)v;
-        l[d] = (float)(v - (double)h[d]);
-      }
+      float h[3] = {0.f, 0.f, 0.f};
+      for (int d = 0; d < dim; ++d) h[d] = (float)(coords_host[(size_t)d * n + i] * sc);
       ph[i] = make_float4(h[0], h[1], h[2], 0.f);
-      pl[i] = make_float4(l[0], l[1], l[2], 0.f);
     }
     MGB_CUDA(cudaMemcpyAsync((void*)S.pts_hi, ph.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s_));
-    MGB_CUDA(cudaMemcpyAsync((void*)S.pts_lo, pl.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s_));
   }
   host_[slot] = S;
   MGB_CUDA(cudaMemcpyAsync(dev_sys_ + slot, &host_[slot], sizeof(BatchSys), cudaMemcpyHostToDevice, s_));

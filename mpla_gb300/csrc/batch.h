@@ -40,8 +40,7 @@ struct BatchSys {
   double* vpart;         // vector-phase partial sums: nvec x 8
   unsigned int* ticket;  // last-arrival counter of the vector phases
   const double* pts64;   // dim x n, structure of arrays
-  const float4* pts_hi;  // mixed: coordinates x sqrt(log2 e), rounded to FP32 ...
-  const float4* pts_lo;  // ... and the FP32 remainder (hi + lo carries ~48 bits)
+  const float4* pts_hi;  // mixed: coordinates x sqrt(log2 e), rounded to FP32
   float* d32;            // mixed: FP32 copy of d
   BatchLane* lanes;      // 8 lanes
 };
