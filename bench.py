@@ -48,6 +48,10 @@ L2_FLUSH_BYTES = 512 << 20
 # reference iterations into solves/s.  Other sizes fall back to the mixed
 # count (a lower bound on the FP64 count for this family).
 FP64_ITERATIONS_N65536 = 18958
+# DRAM bytes (read + write) of one launch of the FP32 group kernel at
+# n = 65536, d = 2 from an ncu capture (profiles/gauss_f32_group_n65536_d2.md):
+# points, slots and x stay in L2
+GROUP_KERNEL_DRAM_BYTES_N65536 = 1.462272e6 + 0.571648e6
 SFU_EX2_PER_CLK_SM = 32.0
 SMI_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -492,7 +496,9 @@ def run_ours(args, world, rank, local):
                  "mixed_over_fp64": value / fp64_solves_est},
         "roofline": {"bound": "sfu", "kernel": "sym_f32_group_kernel (+ gather, reduce)",
                      "achieved": mixed_rate / 1e12, "peak": sfu_peak / 1e12, "unit": "Tex2/s",
-                     "frac": mixed_rate / sfu_peak, "traffic": None,
+                     "frac": mixed_rate / sfu_peak,
+                     "traffic": GROUP_KERNEL_DRAM_BYTES_N65536 if (n == N_FULL and DIM == 2) else None,
+                     "traffic_unit": "DRAM bytes per launch (ncu)",
                      "per_unit": "1 evaluated kernel entry = 1 ex2 (+ ~7 FP32 issue slots); each unordered pair of "
                                  "points evaluated once, tile pairs below 2^-40 skipped",
                      "evaluated_per_launch": evaluated, "algorithmic_entries_per_launch": entries,
