@@ -7,28 +7,36 @@
 // compared with the reference, which builds and multiplies every entry
 // (MPLA src/kernel.cu:118-171, src/generic_system_adapter.cu:83-137).
 //
-//   pair kernel   one CTA per tile pair; 256 threads in a 16 x 16 grid, each
-//                 thread an 8 x 8 register block of entries, with row and
-//                 column accumulators in registers.  Row sums reduce across
-//                 a half-warp with shuffles, column sums across the CTA in
-//                 shared memory.  Each contribution is written to its own
-//                 slot S[tile][other tile][row]: no atomics.
+// FP64 (the plain-CG operator and the mixed CG's true residual):
+//   pair kernel   a fixed grid strides over the tile pairs; 256 threads in a
+//                 16 x 16 grid, each thread an 8 x 8 register block of
+//                 entries, with row and column accumulators in registers.
+//                 Row sums reduce across a half-warp with shuffles, column
+//                 sums across the CTA in shared memory.  Each contribution is
+//                 written to its own slot S[tile][other tile][row]: no
+//                 atomics.
 //   reduce kernel y_i = sum over the T slots of row i in tile order (FP64),
 //                 + nugget x_i: a fixed order, so the product is
 //                 bit-reproducible.
+//   Entries exp(-s) with the table exponential (devutil.cuh) on the squared
+//   distance of the caller's coordinates; 15 FP64 operations per evaluated
+//   entry, 7.5 per matrix entry (d = 2).  Every pair is evaluated.
 //
-// FP64: entries exp(-s) with the table exponential (devutil.cuh) on the
-// squared distance of the caller's coordinates; 15 FP64 operations per
-// evaluated entry, 7.5 per matrix entry (d = 2).
-// FP32: points are Morton-ordered (compact tiles) and rounded to FP32 once
-// per point, so the FP32 operator is exactly the Gaussian kernel matrix of a
-// slightly perturbed point set and stays symmetric positive definite.  (A
-// per-tile-pair centring, with the difference of the two tile centres rounded
-// once per pair, perturbs every tile pair differently; at n = 65536 that
-// operator made the mixed solve stagnate at relres 1.4e-10, so the tile
-// centres are kept at zero here.)  Exponentials on the SFU (ex2.approx, with
-// coordinates pre-scaled by sqrt(log2 e)).  About 8 issue slots and 1 MUFU
-// per evaluated entry, i.e. 0.5 MUFU per matrix entry.
+// FP32 (the mixed CG's operator, MGB_MIXED_SIMT):
+//   group kernel  one CTA per column tile and group of 4 row tiles, packed
+//                 f32x2 arithmetic, tile pairs whose entries are all below
+//                 2^-40 left out (see the kernel);
+//   reduce kernel row slots of the near column tiles and the column slots of
+//                 the groups, in a fixed order.
+//   Points are Morton-ordered (compact tiles) and rounded to FP32 once per
+//   point, so the FP32 operator is the Gaussian kernel matrix of a slightly
+//   perturbed point set and stays symmetric positive definite.  (A
+//   per-tile-pair centring, with the difference of the two tile centres
+//   rounded once per pair, perturbs every tile pair differently; at
+//   n = 65536 that operator made the mixed solve stagnate at relres 1.4e-10,
+//   so coordinates are global.)  Exponentials on the SFU (ex2.approx, with
+//   coordinates pre-scaled by sqrt(log2 e)).  About 8 issue slots and 1 MUFU
+//   per evaluated entry.
 #include <algorithm>
 #include <cmath>
 #include <cstring>

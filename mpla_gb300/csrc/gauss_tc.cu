@@ -1,5 +1,13 @@
 // Symmetric FP32 Gaussian matvec with the squared distances on the tensor
-// cores (tcgen05, sm_103a): the operator of the mixed-precision CG.
+// cores (tcgen05, sm_103a): the MGB_MIXED_TENSOR variant of the mixed-CG
+// operator (mgb_set_mixed_matvec).  Measured against the default
+// (FP32-difference) kernel on GB300 it is slower (1.06 ms against 0.31 ms at
+// n = 65536, d = 2: one tile-pair group per CTA leaves the bulk-copy, MMA and
+// TMEM-allocation latencies exposed), and its errors -- from norms taken
+// relative to a per-tile-pair centre -- are coherent across each 128 x 128
+// block, enough at n = 65536 to make the FP32 operator indefinite at a 1e-4
+// nugget.  It is kept as the tensor-core form of the operator, tested to the
+// same matvec bar on moderate tile extents.
 //
 // Points are in Morton order, in 128-point tiles.  One CTA takes a column
 // tile J and two row tiles I0 = 2g, I0 + 1 <= J.  Relative to the column
