@@ -40,7 +40,7 @@ def _gauss(n, dim, ell, precision, reps):
     y = mg.DeviceArray(n)
     ms = mg.time_gauss_matvec(dp, 1e-4, precision, x.ptr, y.ptr, reps=reps)
     name = "fp64" if precision == mg.PREC_FP64 else "mixed"
-    print(f"gauss_{name} n={n} d={dim}: {ms:.4f} ms/launch, {float(n) * n / ms / 1e9:.2f} Gentries/s")
+    print(f"gauss_{name} n={n} d={dim}: {ms:.4f} ms/launch, {float(n) * n / ms / 1e6:.2f} Gentries/s")
 
 
 def case_gauss_f64(reps=2):
