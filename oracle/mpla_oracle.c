@@ -268,7 +268,7 @@ int orc_bicgstab(const orc_operator* op, const double* b, double* x, int iter_ma
 }
 
 /* ||b - A x|| / ||b|| in FP64: the true relative residual against which the
- * mixed-precision solver is judged. */
+ * mixed-precision solver is checked. */
 double orc_true_relres(const orc_operator* op, const double* b, const double* x) {
   const int n = op->n;
   double* z = (double*)malloc(sizeof(double) * n);

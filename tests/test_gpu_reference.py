@@ -2,7 +2,7 @@
 
 The reference is compiled from its own sources (oracle/build_ref.py) and
 called through its public API (oracle/ref_harness.cu).  Same seeded inputs
-on both sides: dgemv to 1e-13 relative (the benchmark spec), kernel matvecs to 1e-13,
+on both sides: dgemv to 1e-13 relative, kernel matvecs to 1e-13,
 dense CG iteration counts +-1, the Gaussian CG family within 1 % (nugget
 1e-2) and 3 % (nugget 1e-4), BiCGSTAB within 20 %.
 """
