@@ -1,6 +1,6 @@
 """dgemv / ddot / daxpy on the GPU against the oracle and the reference KAT.
 
-Bar: relative 1e-13 for dgemv (the benchmark spec), measured against sum_j |A_ij x_j|
+Bar: relative 1e-13 for dgemv (the parity bar of this path), measured against sum_j |A_ij x_j|
 so cancellation in a row does not inflate it; the reference's own
 known-answer test (test_library.cpp) at 1e-13 instead of its 1e-12.
 """
