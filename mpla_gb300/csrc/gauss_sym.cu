@@ -284,16 +284,14 @@ __device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
 // is below 2^-40, so even summed over all n columns a row loses less than
 // n * 2^-40 (6e-8 at n = 65536) -- far below the FP32 rounding of its sum and
 // the nugget.  The CTA map lists only groups with a near row tile, and a
-// 4-bit mask per CTA marks which of its row tiles are near, and a 16-bit
-// mask which (row tile, 32-column warp share) combinations are within the
-// cut (the warp's 32 points' bounding box against the row tile's); the
-// slots of far pairs are zeroed once and never written.
+// 4-bit mask per CTA marks which of its row tiles are near; the slots of
+// far pairs are zeroed once and never written.
 constexpr int kGroup = 4;
 constexpr double kFarLog2 = 40.0;
 
 template <int DIM>
 __global__ void __launch_bounds__(kF32Threads) sym_f32_group_kernel(int n, int T, int GT,
-                                                                    const int4* __restrict__ map,
+                                                                    const int2* __restrict__ map,
                                                                     const float4* __restrict__ pts,
                                                                     const float* __restrict__ xf,
                                                                     float* __restrict__ Srow,
@@ -303,8 +301,8 @@ __global__ void __launch_bounds__(kF32Threads) sym_f32_group_kernel(int n, int T
   __shared__ ulonglong2 cq[kB];  // {x, x} {y, y} as packed pairs
   __shared__ ulonglong2 cw[kB];  // {z, z} {x_t, x_t}
   __shared__ float rowacc[kGroup][4][kB];
-  const int4 jm = map[blockIdx.x];
-  const int J = jm.x, g = jm.y, near = jm.z, wmask = jm.w;
+  const int2 jm = map[blockIdx.x];
+  const int J = jm.x, g = jm.y & 0xFFFF, near = jm.y >> 16;
   const int I0 = kGroup * g, I1 = min(I0 + kGroup - 1, J);
   {
     const int t = threadIdx.x;  // 128 threads, 128 columns
@@ -322,8 +320,6 @@ __global__ void __launch_bounds__(kF32Threads) sym_f32_group_kernel(int n, int T
 #pragma unroll 1
   for (int I = I0; I <= I1; ++I) {
     if (!((near >> (I - I0)) & 1)) continue;
-    // this warp's 32 columns may all lie beyond the cut from row tile I
-    const bool mine = (wmask >> (4 * (I - I0) + warp)) & 1;
     uint64_t rx[2], ry[2], rz[2], xi2[2], acc[2];
     const bool diag = I == J;
 #pragma unroll
@@ -338,7 +334,6 @@ __global__ void __launch_bounds__(kF32Threads) sym_f32_group_kernel(int n, int T
       xi2[q] = f2_pack(wa, wb);
       acc[q] = 0ull;  // +0.0f in both halves
     }
-    if (mine) {
 #pragma unroll
     for (int b = 0; b < 32; ++b) {
       const ulonglong2 q2 = cq[32 * warp + b];
@@ -368,7 +363,6 @@ __global__ void __launch_bounds__(kF32Threads) sym_f32_group_kernel(int n, int T
       float c0, c1;
       f2_unpack(c2, c0, c1);
       col[b] = c0 + c1;
-    }
     }
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
@@ -564,52 +558,25 @@ int SymF32::init(DeviceContext* c, const GaussSystem& g, cudaStream_t s) {
       bhi[3 * t + d] = hi;
     }
   }
-  // the same for each tile's four 32-point column shares (one per warp)
-  std::vector<double> qlo((size_t)12 * T_, 0.0), qhi((size_t)12 * T_, 0.0);
-  for (int t = 0; t < T_; ++t)
-    for (int w = 0; w < 4; ++w) {
-      const int b0 = t * kB + 32 * w, b1 = std::min(n_, b0 + 32);
-      for (int d = 0; d < 3; ++d) {
-        double lo = 1e300, hi = -1e300;
-        for (int k = b0; k < b1; ++k) {
-          const float4 q = pts[k];
-          const double v = d == 0 ? q.x : (d == 1 ? q.y : q.z);
-          lo = std::min(lo, v);
-          hi = std::max(hi, v);
-        }
-        qlo[12 * t + 3 * w + d] = lo;
-        qhi[12 * t + 3 * w + d] = hi;
-      }
-    }
-  auto gap2 = [](const double* alo, const double* ahi, const double* blo_, const double* bhi_) {
+  auto far = [&](int a, int b) {
     double d2 = 0.0;
     for (int d = 0; d < 3; ++d) {
-      const double gap = std::max({0.0, blo_[d] - ahi[d], alo[d] - bhi_[d]});
+      const double gap = std::max({0.0, blo[3 * b + d] - bhi[3 * a + d], blo[3 * a + d] - bhi[3 * b + d]});
       d2 += gap * gap;
     }
-    return d2;
+    return d2 > kFarLog2;
   };
-  auto far = [&](int a, int b) { return gap2(&blo[3 * a], &bhi[3 * a], &blo[3 * b], &bhi[3 * b]) > kFarLog2; };
-  auto far_share = [&](int I, int J, int w) {
-    if (std::min(n_, J * kB + 32 * w + 32) <= J * kB + 32 * w) return true;  // no points in this share
-    return gap2(&blo[3 * I], &bhi[3 * I], &qlo[12 * J + 3 * w], &qhi[12 * J + 3 * w]) > kFarLog2;
-  };
-  std::vector<int4> map;
-  evaluated_ = 0;
+  std::vector<int2> map;
+  pairs_near_ = 0;
   for (int J = 0; J < T_; ++J)
     for (int g = 0; g <= J / kGroup; ++g) {
-      int near = 0, wmask = 0;
-      for (int i = 0; i < kGroup && kGroup * g + i <= J; ++i) {
-        const int I = kGroup * g + i;
-        if (far(I, J)) continue;
-        near |= 1 << i;
-        for (int w = 0; w < 4; ++w)
-          if (!far_share(I, J, w)) {
-            wmask |= 1 << (4 * i + w);
-            evaluated_ += 128LL * 32LL;
-          }
-      }
-      if (near) map.push_back(make_int4(J, g, near, wmask));
+      int near = 0;
+      for (int i = 0; i < kGroup && kGroup * g + i <= J; ++i)
+        if (!far(kGroup * g + i, J)) {
+          near |= 1 << i;
+          ++pairs_near_;
+        }
+      if (near) map.push_back(make_int2(J, g | (near << 16)));
     }
   // per row tile I: the column tiles J >= I it is near, ascending
   std::vector<int> near_off(T_ + 1, 0), near_J;
@@ -622,11 +589,11 @@ int SymF32::init(DeviceContext* c, const GaussSystem& g, cudaStream_t s) {
   if (ncta_ > 0x7fffffffLL) return set_error(MGB_ERR_ARG, "system too large for one grid");
   auto up = [](size_t b) { return (b + 255) & ~size_t(255); };
   const size_t bytes_pts = sizeof(float4) * pts.size();
-  const size_t bytes_map = sizeof(int4) * map.size();
+  const size_t bytes_map = sizeof(int2) * map.size();
   const size_t bytes_perm = sizeof(int) * (size_t)n_;
   const size_t bytes_off = sizeof(int) * near_off.size(), bytes_nj = sizeof(int) * std::max<size_t>(1, near_J.size());
   MGB_TRY(pool_alloc(c, up(bytes_pts) + up(bytes_map) + up(bytes_perm) + up(bytes_off) + up(bytes_nj), (void**)&pts_));
-  map_ = reinterpret_cast<int4*>(reinterpret_cast<char*>(pts_) + up(bytes_pts));
+  map_ = reinterpret_cast<int2*>(reinterpret_cast<char*>(pts_) + up(bytes_pts));
   perm_ = reinterpret_cast<int*>(reinterpret_cast<char*>(map_) + up(bytes_map));
   near_off_ = reinterpret_cast<int*>(reinterpret_cast<char*>(perm_) + up(bytes_perm));
   near_J_ = reinterpret_cast<int*>(reinterpret_cast<char*>(near_off_) + up(bytes_off));

@@ -36,16 +36,16 @@ class SymF32 : public Matvec {
   int apply(const double* x, double* y, cudaStream_t s, const int* skip) override;
   int n() const override { return n_; }
   // kernel entries (exponentials) one apply evaluates
-  long long evaluated() const { return evaluated_; }
+  long long evaluated() const { return pairs_near_ * 128LL * 128LL; }
 
  private:
   DeviceContext* c_ = nullptr;
   int n_ = 0, dim_ = 0, T_ = 0, GT_ = 0;
   long long ncta_ = 0;
-  long long evaluated_ = 0;   // entries evaluated per apply (far tile pairs and warp shares left out)
+  long long pairs_near_ = 0;  // tile pairs I <= J evaluated (the rest are below 2^-40)
   double nugget_ = 0.0;
   float4* pts_ = nullptr;     // T*128 scaled FP32 points (pool block, also holds map_ and perm_)
-  int4* map_ = nullptr;       // CTA -> (column tile, row-tile group, near-tile mask, warp-share mask)
+  int2* map_ = nullptr;       // CTA -> (column tile, row-tile group | near mask << 16)
   int* perm_ = nullptr;       // sorted position -> original index
   int* near_off_ = nullptr;   // per row tile I: offsets into near_J_
   int* near_J_ = nullptr;     // column tiles J >= I near tile I
