@@ -9,11 +9,11 @@
 //
 // One step (captured once into a CUDA graph, replayed until every lane is
 // done):
-//   mv32    persistent kernel over (system, 128 rows, 2048-column chunk)
+//   mv32    persistent kernel over (system, 128 rows, 1024-column chunk)
 //           items of mixed systems: partial K~ d per chunk, entries in FP32
-//           with the exponential on the SFU, 128-column sums in FP32 added
-//           into FP64
+//           with the exponential on the SFU, summed in FP32 per chunk
 //   mv64    the same items of FP64 systems: partial K d in FP64
+//           (the matvecs of every class and mode run as concurrent branches)
 //   alpha   persistent kernel over (system, 1024-row) items: z = nugget d +
 //           the chunk partials in chunk order, per-item <d,z>; the last item
 //           of a system to finish sums the items in order and sets alpha
@@ -61,7 +61,7 @@ namespace {
 
 constexpr int kTile = 128;        // rows per item and threads per matvec CTA
 constexpr int kColTile = 128;     // columns staged per shared-memory round
-constexpr int kChunkCols = 2048;  // columns per matvec item
+constexpr int kChunkCols = 1024;  // columns per matvec item
 constexpr int kVecThreads = 256;  // threads of the vector-phase CTAs
 constexpr int kVecRows = 1024;    // rows per vector-phase item
 
@@ -131,12 +131,19 @@ __device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
   asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
   return r;
 }
+__device__ __forceinline__ uint64_t f2_add(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
 
 // Partial (K~ d) over one column chunk for the R lanes of mixed systems of one
 // class, into P[chunk].  A thread owns RPT rows (RPT/2 packed pairs: rows r
 // and r + 128 of a pair of tiles); column values are staged in shared memory
 // twice over so that one load gives a packed operand.  Per 128-column tile
-// the products are summed in FP32, and the tile sums in FP64.
+// the products are summed in FP32, the tile sums of the chunk in FP32 as
+// well (no FP64 work inside the chunk: GB300's FP64 pipe issues ~2 operations
+// per clock per SM), and each chunk partial is stored in FP64.
 template <int DIM, int R, int RPT>
 __global__ void __launch_bounds__(kTile) k_bmv32(WorkQueue q, const BatchSys* __restrict__ sys) {
   constexpr int NP = RPT / 2;  // packed row pairs per thread
@@ -165,11 +172,11 @@ __global__ void __launch_bounds__(kTile) k_bmv32(WorkQueue q, const BatchSys* __
       hy[p] = f2_pack(h0.y, h1.y);
       hz[p] = f2_pack(h0.z, h1.z);
     }
-    double acc[RPT][R];
+    uint64_t acc[NP][R];  // chunk sums, packed FP32
 #pragma unroll
-    for (int a = 0; a < RPT; ++a)
+    for (int p = 0; p < NP; ++p)
 #pragma unroll
-      for (int k = 0; k < R; ++k) acc[a][k] = 0.0;
+      for (int k = 0; k < R; ++k) acc[p][k] = 0ull;
     const int c0 = w.chunk * kChunkCols, c1 = min(n, c0 + kChunkCols);
     for (int j0 = c0; j0 < c1; j0 += kColTile) {
       const int nj = min(kColTile, c1 - j0);
@@ -227,18 +234,16 @@ __global__ void __launch_bounds__(kTile) k_bmv32(WorkQueue q, const BatchSys* __
 #pragma unroll
       for (int p = 0; p < NP; ++p)
 #pragma unroll
-        for (int k = 0; k < R; ++k) {
-          float a0, a1;
-          f2_unpack(part[p][k], a0, a1);
-          acc[2 * p][k] += (double)a0;
-          acc[2 * p + 1][k] += (double)a1;
-        }
+        for (int k = 0; k < R; ++k) acc[p][k] = f2_add(acc[p][k], part[p][k]);
     }
 #pragma unroll
-    for (int a = 0; a < RPT; ++a) {
-      if (row[a] < n) {
+    for (int p = 0; p < NP; ++p) {
 #pragma unroll
-        for (int k = 0; k < R; ++k) S.P[((long long)w.chunk * n + row[a]) * R + k] = acc[a][k];
+      for (int k = 0; k < R; ++k) {
+        float a0, a1;
+        f2_unpack(acc[p][k], a0, a1);
+        if (row[2 * p] < n) S.P[((long long)w.chunk * n + row[2 * p]) * R + k] = (double)a0;
+        if (row[2 * p + 1] < n) S.P[((long long)w.chunk * n + row[2 * p + 1]) * R + k] = (double)a1;
       }
     }
   }
@@ -652,7 +657,7 @@ int BatchEngine::init(DeviceContext* c, int max_systems, cudaStream_t s) {
   blocks_.assign(max_systems, nullptr);
   MGB_TRY(pool_alloc(c, sizeof(BatchSys) * max_systems, (void**)&dev_sys_));
   MGB_CUDA(cudaMemsetAsync(dev_sys_, 0, sizeof(BatchSys) * max_systems, s));
-  max_items_ = 1 << 18;
+  max_items_ = 1 << 19;  // 256 systems of n = 16384 in one class
   for (int q = 0; q < kClasses; ++q) {
     MGB_TRY(pool_alloc(c, sizeof(BatchItem) * max_items_, (void**)&items_[q]));
     items_host_[q].clear();
@@ -662,6 +667,11 @@ int BatchEngine::init(DeviceContext* c, int max_systems, cudaStream_t s) {
   MGB_TRY(pool_alloc(c, sizeof(int) * kCounterInts, (void**)&counters_));
   MGB_CUDA(cudaMemsetAsync(counters_, 0, sizeof(int) * kCounterInts, s));
   MGB_CUDA(cudaMallocHost(&active_host_, sizeof(int)));
+  MGB_CUDA(cudaEventCreateWithFlags(&fork_ev_, cudaEventDisableTiming));
+  for (int i = 0; i < kBranches; ++i) {
+    MGB_CUDA(cudaStreamCreateWithFlags(&side_[i], cudaStreamNonBlocking));
+    MGB_CUDA(cudaEventCreateWithFlags(&join_ev_[i], cudaEventDisableTiming));
+  }
   for (int k = 0; k < kClasses; ++k) rpt_[k] = 0;
   MGB_CUDA(cudaStreamSynchronize(s));
   return MGB_OK;
@@ -680,6 +690,11 @@ BatchEngine::~BatchEngine() {
   if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
   if (graph_) cudaGraphDestroy(graph_);
   if (active_host_) cudaFreeHost(active_host_);
+  for (int i = 0; i < kBranches; ++i) {
+    if (side_[i]) cudaStreamDestroy(side_[i]);
+    if (join_ev_[i]) cudaEventDestroy(join_ev_[i]);
+  }
+  if (fork_ev_) cudaEventDestroy(fork_ev_);
 }
 
 int BatchEngine::class_of(int dim, int R) {
@@ -854,18 +869,18 @@ static void launch_mv32(const WorkQueue& q, const BatchSys* sys, int rpt, int gr
   else k_bmv32<DIM, R, 2><<<grid, kTile, 0, s>>>(q, sys);
 }
 
-int BatchEngine::enqueue_mv32(int cls, int rpt) {
+int BatchEngine::enqueue_mv32(int cls, int rpt, cudaStream_t s) {
   const WorkQueue q = make_queue(items_[cls], counters_, cls, Q_MV32);
   const int grid = 4 * c_->num_sms;
   switch (cls) {
-    case 0: launch_mv32<2, 1>(q, dev_sys_, rpt, grid, s_); break;
-    case 1: launch_mv32<2, 2>(q, dev_sys_, rpt, grid, s_); break;
-    case 2: launch_mv32<2, 4>(q, dev_sys_, rpt, grid, s_); break;
-    case 3: launch_mv32<2, 8>(q, dev_sys_, rpt, grid, s_); break;
-    case 4: launch_mv32<3, 1>(q, dev_sys_, rpt, grid, s_); break;
-    case 5: launch_mv32<3, 2>(q, dev_sys_, rpt, grid, s_); break;
-    case 6: launch_mv32<3, 4>(q, dev_sys_, rpt, grid, s_); break;
-    default: launch_mv32<3, 8>(q, dev_sys_, rpt, grid, s_); break;
+    case 0: launch_mv32<2, 1>(q, dev_sys_, rpt, grid, s); break;
+    case 1: launch_mv32<2, 2>(q, dev_sys_, rpt, grid, s); break;
+    case 2: launch_mv32<2, 4>(q, dev_sys_, rpt, grid, s); break;
+    case 3: launch_mv32<2, 8>(q, dev_sys_, rpt, grid, s); break;
+    case 4: launch_mv32<3, 1>(q, dev_sys_, rpt, grid, s); break;
+    case 5: launch_mv32<3, 2>(q, dev_sys_, rpt, grid, s); break;
+    case 6: launch_mv32<3, 4>(q, dev_sys_, rpt, grid, s); break;
+    default: launch_mv32<3, 8>(q, dev_sys_, rpt, grid, s); break;
   }
   count_launches(1);
   MGB_CUDA(cudaGetLastError());
@@ -879,20 +894,20 @@ static void launch_mv64(const WorkQueue& q, const BatchSys* sys, bool true_res, 
   else k_bmv64<DIM, R, false><<<grid, kTile, 0, s>>>(q, sys, table);
 }
 
-int BatchEngine::enqueue_mv64(int cls, int mode) {
+int BatchEngine::enqueue_mv64(int cls, int mode, cudaStream_t s) {
   const WorkQueue q = make_queue(items_[cls], counters_, cls, mode);
   const int grid = 2 * c_->num_sms;
   const double* t = c_->exp_table;
   const bool tr = mode == Q_MV64_TRUE;
   switch (cls) {
-    case 0: launch_mv64<2, 1>(q, dev_sys_, tr, t, grid, s_); break;
-    case 1: launch_mv64<2, 2>(q, dev_sys_, tr, t, grid, s_); break;
-    case 2: launch_mv64<2, 4>(q, dev_sys_, tr, t, grid, s_); break;
-    case 3: launch_mv64<2, 8>(q, dev_sys_, tr, t, grid, s_); break;
-    case 4: launch_mv64<3, 1>(q, dev_sys_, tr, t, grid, s_); break;
-    case 5: launch_mv64<3, 2>(q, dev_sys_, tr, t, grid, s_); break;
-    case 6: launch_mv64<3, 4>(q, dev_sys_, tr, t, grid, s_); break;
-    default: launch_mv64<3, 8>(q, dev_sys_, tr, t, grid, s_); break;
+    case 0: launch_mv64<2, 1>(q, dev_sys_, tr, t, grid, s); break;
+    case 1: launch_mv64<2, 2>(q, dev_sys_, tr, t, grid, s); break;
+    case 2: launch_mv64<2, 4>(q, dev_sys_, tr, t, grid, s); break;
+    case 3: launch_mv64<2, 8>(q, dev_sys_, tr, t, grid, s); break;
+    case 4: launch_mv64<3, 1>(q, dev_sys_, tr, t, grid, s); break;
+    case 5: launch_mv64<3, 2>(q, dev_sys_, tr, t, grid, s); break;
+    case 6: launch_mv64<3, 4>(q, dev_sys_, tr, t, grid, s); break;
+    default: launch_mv64<3, 8>(q, dev_sys_, tr, t, grid, s); break;
   }
   count_launches(1);
   MGB_CUDA(cudaGetLastError());
@@ -918,15 +933,44 @@ int BatchEngine::enqueue_vec(int phase) {
   return MGB_OK;
 }
 
-int BatchEngine::enqueue_step() {
-  for (int cls = 0; cls < kClasses; ++cls) {
-    if (has_mixed_[cls]) MGB_TRY(enqueue_mv32(cls, rpt_[cls] ? rpt_[cls] : 2));
-    if (has_fp64_[cls]) MGB_TRY(enqueue_mv64(cls, Q_MV64));
+// The matvec launches of one phase (one per class and mode) touch disjoint
+// systems and queues, so they run as parallel branches: each on its own side
+// stream, forked from and joined back into the engine stream.  Under stream
+// capture this becomes a fan-out / fan-in of graph nodes, and the GPU fills
+// the tail of one class's launch with the items of the others.
+int BatchEngine::fork_branches(int nb) {
+  MGB_CUDA(cudaEventRecord(fork_ev_, s_));
+  for (int i = 0; i < nb; ++i) MGB_CUDA(cudaStreamWaitEvent(side_[i], fork_ev_, 0));
+  return MGB_OK;
+}
+
+int BatchEngine::join_branches(int nb) {
+  for (int i = 0; i < nb; ++i) {
+    MGB_CUDA(cudaEventRecord(join_ev_[i], side_[i]));
+    MGB_CUDA(cudaStreamWaitEvent(s_, join_ev_[i], 0));
   }
+  return MGB_OK;
+}
+
+int BatchEngine::enqueue_step() {
+  int nb = 0;
+  for (int cls = 0; cls < kClasses; ++cls) nb += (int)has_mixed_[cls] + (int)has_fp64_[cls];
+  MGB_TRY(fork_branches(nb));
+  nb = 0;
+  for (int cls = 0; cls < kClasses; ++cls) {
+    if (has_mixed_[cls]) MGB_TRY(enqueue_mv32(cls, rpt_[cls] ? rpt_[cls] : 2, side_[nb++]));
+    if (has_fp64_[cls]) MGB_TRY(enqueue_mv64(cls, Q_MV64, side_[nb++]));
+  }
+  MGB_TRY(join_branches(nb));
   MGB_TRY(enqueue_vec(0));
   MGB_TRY(enqueue_vec(1));
+  nb = 0;
+  for (int cls = 0; cls < kClasses; ++cls) nb += (int)has_mixed_[cls];
+  MGB_TRY(fork_branches(nb));
+  nb = 0;
   for (int cls = 0; cls < kClasses; ++cls)
-    if (has_mixed_[cls]) MGB_TRY(enqueue_mv64(cls, Q_MV64_TRUE));
+    if (has_mixed_[cls]) MGB_TRY(enqueue_mv64(cls, Q_MV64_TRUE, side_[nb++]));
+  MGB_TRY(join_branches(nb));
   MGB_TRY(enqueue_vec(2));
   MGB_TRY(enqueue_vec(3));
   k_bcount<<<1, 256, 0, s_>>>(dev_sys_, nslots_, counters_ + kOffActive);
@@ -952,13 +996,13 @@ int BatchEngine::autotune() {
     int best_rpt = 2;
     for (int v = 1; v < 3 && st == MGB_OK; ++v) {
       const int rpt = 1 << v;
-      st = enqueue_mv32(cls, rpt);  // warm-up
+      st = enqueue_mv32(cls, rpt, s_);  // warm-up
       if (st != MGB_OK) break;
       if (cudaEventRecord(e0, s_) != cudaSuccess) {
         st = set_error(MGB_ERR_CUDA, "batch autotune: event failure");
         break;
       }
-      st = enqueue_mv32(cls, rpt);
+      st = enqueue_mv32(cls, rpt, s_);
       if (st != MGB_OK) break;
       if (cudaEventRecord(e1, s_) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
         st = set_error(MGB_ERR_CUDA, "batch autotune: event failure");

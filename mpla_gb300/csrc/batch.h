@@ -62,6 +62,7 @@ class BatchEngine {
  public:
   static constexpr int kClasses = 8;        // (dim 2|3) x (R 1|2|4|8)
   static constexpr int kStepsPerGraph = 8;  // CG iterations per graph replay
+  static constexpr int kBranches = 2 * kClasses;  // concurrent matvec launches of a phase
   // device counters: matvec queues (claim, finished) per class and mode,
   // item counts per class, the active-system count, vector-phase queues
   // (claim, finished) per phase and the vector item count
@@ -89,8 +90,10 @@ class BatchEngine {
   int sync_items();
   int autotune();
   int enqueue_step();
-  int enqueue_mv32(int cls, int rpt);
-  int enqueue_mv64(int cls, int mode);
+  int fork_branches(int nb);
+  int join_branches(int nb);
+  int enqueue_mv32(int cls, int rpt, cudaStream_t s);
+  int enqueue_mv64(int cls, int mode, cudaStream_t s);
   int enqueue_vec(int phase);
 
   DeviceContext* c_ = nullptr;
@@ -114,6 +117,9 @@ class BatchEngine {
   int* active_host_ = nullptr;
   int rpt_[kClasses] = {};
   float tune_ms_[kClasses][3] = {};
+  cudaStream_t side_[kBranches] = {};
+  cudaEvent_t join_ev_[kBranches] = {};
+  cudaEvent_t fork_ev_ = nullptr;
   cudaGraph_t graph_ = nullptr;
   cudaGraphExec_t graph_exec_ = nullptr;
   unsigned int graph_sig_ = 0;

@@ -8,6 +8,7 @@ that ends by itself (a few hundred MB on the device at most):
   python -m mpla_gb300.profile_cases gauss_mixed # FP32/SFU Gaussian matvec, n = 65536, d = 2
   python -m mpla_gb300.profile_cases mixed_cg    # 300 mixed-CG iterations, n = 16384, d = 2
   python -m mpla_gb300.profile_cases batch       # 100 steps of a 24-system batch (n <= 4096)
+  python -m mpla_gb300.profile_cases batch128    # 16 timed steps of 128 batch systems (n <= 16384)
   python -m mpla_gb300.profile_cases mixed_c3    # full mixed solve, n = 131072, d = 3, l = 0.08
   python -m mpla_gb300.profile_cases all
 
@@ -78,6 +79,28 @@ def case_batch(steps=100):
     batch.close()
 
 
+def case_batch128(steps=16):
+    """The batch workload's step at its busiest: the first 128 of the 512
+    systems (n log-uniform in [256, 16384]) admitted together, one warm-up
+    replay, then `steps` timed iterations (host wall time around whole graph
+    replays, which end with a device synchronisation)."""
+    import time
+
+    spec = synth.batch_spec(512)
+    batch = mg.Batch(128)
+    for k in range(128):
+        g = synth.batch_system(spec, k)
+        batch.add(g.scaled(), g.nugget, g.b, precision=mg.PREC_MIXED)
+    batch.run(max_steps=8)
+    t0 = time.perf_counter()
+    active = batch.run(max_steps=steps)
+    ms = (time.perf_counter() - t0) * 1e3 / steps
+    rpt, tune = batch.tuning()
+    print(f"batch128: {ms:.3f} ms per step, {active} of 128 systems running, rows per thread {rpt}, "
+          f"FP32 matvec ms per class (2 / 4 rows per thread) {[[round(t, 4) for t in c[1:]] for c in tune]}")
+    batch.close()
+
+
 def case_mixed_c3():
     """The mixed-precision configuration: n = 131072 points U[0,1]^3, l = 0.08,
     nugget 1e-4, b = sin(2 pi x1) cos(2 pi x2), solved to relres 1e-10."""
@@ -101,12 +124,12 @@ def case_mixed_c3():
 
 
 CASES = {"dgemv": case_dgemv, "gauss_f64": case_gauss_f64, "gauss_mixed": case_gauss_mixed,
-         "mixed_cg": case_mixed_cg, "batch": case_batch, "mixed_c3": case_mixed_c3}
+         "mixed_cg": case_mixed_cg, "batch": case_batch, "batch128": case_batch128, "mixed_c3": case_mixed_c3}
 
 
 def main(argv):
     mg.init(0)
-    names = [k for k in CASES if k != "mixed_c3"] if (not argv or argv[0] == "all") else argv
+    names = [k for k in CASES if k not in ("mixed_c3", "batch128")] if (not argv or argv[0] == "all") else argv
     for name in names:
         CASES[name]()
     mg.synchronize()
