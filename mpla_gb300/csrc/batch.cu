@@ -657,11 +657,13 @@ int BatchEngine::init(DeviceContext* c, int max_systems, cudaStream_t s) {
   blocks_.assign(max_systems, nullptr);
   MGB_TRY(pool_alloc(c, sizeof(BatchSys) * max_systems, (void**)&dev_sys_));
   MGB_CUDA(cudaMemsetAsync(dev_sys_, 0, sizeof(BatchSys) * max_systems, s));
-  max_items_ = 1 << 19;  // 256 systems of n = 16384 in one class
-  for (int q = 0; q < kClasses; ++q) {
-    MGB_TRY(pool_alloc(c, sizeof(BatchItem) * max_items_, (void**)&items_[q]));
-    items_host_[q].clear();
-  }
+  max_items_ = 1 << 18;  // 128 systems of n = 16384 in one class
+  listed_.assign(max_systems, 0);
+  listed_count_ = 0;
+  for (int l = 0; l < kLists; ++l)
+    for (int q = 0; q < kClasses; ++q)
+      MGB_TRY(pool_alloc(c, sizeof(BatchItem) * list_capacity(l), (void**)&items_[l][q]));
+  for (int q = 0; q < kClasses; ++q) items_host_[q].clear();
   MGB_TRY(pool_alloc(c, sizeof(VecItem) * max_items_, (void**)&vitems_));
   vitems_host_.clear();
   MGB_TRY(pool_alloc(c, sizeof(int) * kCounterInts, (void**)&counters_));
@@ -681,9 +683,10 @@ BatchEngine::~BatchEngine() {
   if (!c_) return;
   cudaStreamSynchronize(s_);
   for (int i = 0; i < max_; ++i)
-    if (host_[i].in_use) release_slot(i);
-  for (int q = 0; q < kClasses; ++q)
-    if (items_[q]) pool_free(c_, items_[q]);
+    if (host_[i].in_use) pool_free(c_, blocks_[i]);
+  for (int l = 0; l < kLists; ++l)
+    for (int q = 0; q < kClasses; ++q)
+      if (items_[l][q]) pool_free(c_, items_[l][q]);
   if (vitems_) pool_free(c_, vitems_);
   if (counters_) pool_free(c_, counters_);
   if (dev_sys_) pool_free(c_, dev_sys_);
@@ -733,10 +736,22 @@ int BatchEngine::add(int n, int dim, const double* coords_host, double nugget, i
   const int R = padded_rhs(nrhs);
   const int cls = class_of(dim, R);
   const int nchunks = chunks_of(n), nvec = vec_items_of(n);
-  const long long new_items = (long long)((n + kTile - 1) / kTile) * nchunks;
-  if ((long long)items_host_[cls].size() + new_items > max_items_ ||
-      (long long)vitems_host_.size() + nvec > max_items_)
-    return set_error(MGB_ERR_NOMEM, "batch add: more than %d work items", max_items_);
+  {
+    const long long tiles = (n + kTile - 1) / kTile;
+    const long long add_items[kLists] = {tiles * nchunks, (tiles + 1) / 2 * nchunks, (tiles + 3) / 4 * nchunks,
+                                         tiles};
+    long long have[kLists] = {};
+    for (const BatchItem& w : items_host_[cls]) {
+      const int t = w.row0 / kTile;
+      have[kListAll] += 1;
+      have[kListRpt2] += t % 2 == 0;
+      have[kListRpt4] += t % 4 == 0;
+      have[kListTrue] += w.chunk == 0;
+    }
+    bool fits = (long long)vitems_host_.size() + nvec <= max_items_;
+    for (int l = 0; l < kLists; ++l) fits = fits && have[l] + add_items[l] <= list_capacity(l);
+    if (!fits) return set_error(MGB_ERR_NOMEM, "batch add: more than %d work items", max_items_);
+  }
   // admission by free device memory
   const size_t need = bytes_needed(n, dim, nrhs, precision);
   size_t free_b = 0, total_b = 0;
@@ -807,37 +822,80 @@ int BatchEngine::add(int n, int dim, const double* coords_host, double nugget, i
   for (int r0 = 0; r0 < n; r0 += kTile)
     for (int c = 0; c < nchunks; ++c) items_host_[cls].push_back(BatchItem{slot, r0, c});
   for (int r0 = 0; r0 < n; r0 += kVecRows) vitems_host_.push_back(VecItem{slot, r0});
+  listed_[slot] = 1;
+  listed_count_ += 1;
   items_dirty_ = true;
   nslots_ = std::max(nslots_, slot + 1);
   *handle = slot;
   return MGB_OK;
 }
 
+// Takes the work items of the slots marked in `drop` out of the lists (their
+// systems are finished or released: every kernel would skip them).
+void BatchEngine::unlist(const std::vector<char>& drop) {
+  for (int q = 0; q < kClasses; ++q) {
+    auto& v = items_host_[q];
+    v.erase(std::remove_if(v.begin(), v.end(), [&](const BatchItem& w) { return drop[w.sys] != 0; }), v.end());
+  }
+  vitems_host_.erase(std::remove_if(vitems_host_.begin(), vitems_host_.end(),
+                                    [&](const VecItem& w) { return drop[w.sys] != 0; }),
+                     vitems_host_.end());
+  for (int i = 0; i < max_; ++i)
+    if (drop[i] && listed_[i]) {
+      listed_[i] = 0;
+      listed_count_ -= 1;
+    }
+  items_dirty_ = true;
+}
+
 void BatchEngine::release_slot(int slot) {
   pool_free(c_, blocks_[slot]);
   blocks_[slot] = nullptr;
-  const int cls = class_of(host_[slot].dim, host_[slot].R);
-  auto& v = items_host_[cls];
-  v.erase(std::remove_if(v.begin(), v.end(), [&](const BatchItem& w) { return w.sys == slot; }), v.end());
-  vitems_host_.erase(std::remove_if(vitems_host_.begin(), vitems_host_.end(),
-                                    [&](const VecItem& w) { return w.sys == slot; }),
-                     vitems_host_.end());
+  if (listed_[slot]) {
+    std::vector<char> drop(max_, 0);
+    drop[slot] = 1;
+    unlist(drop);
+  }
   host_[slot] = BatchSys{};
-  items_dirty_ = true;
+}
+
+// After a replay in which systems finished: read their lane state and drop
+// the finished systems' items, so that later steps no longer claim and skip
+// them (their results stay in place until read).
+int BatchEngine::prune_finished() {
+  std::vector<BatchSys> snap(nslots_);
+  MGB_CUDA(cudaMemcpyAsync(snap.data(), dev_sys_, sizeof(BatchSys) * nslots_, cudaMemcpyDeviceToHost, s_));
+  MGB_CUDA(cudaStreamSynchronize(s_));
+  std::vector<char> drop(max_, 0);
+  bool any = false;
+  for (int i = 0; i < nslots_; ++i)
+    if (listed_[i] && snap[i].in_use && snap[i].active_lanes == 0) drop[i] = 1, any = true;
+  if (any) unlist(drop);
+  return MGB_OK;
 }
 
 int BatchEngine::sync_items() {
   if (!items_dirty_) return MGB_OK;
   for (int q = 0; q < kClasses; ++q) {
-    const int cnt = (int)items_host_[q].size();
-    if (cnt)
-      MGB_CUDA(cudaMemcpyAsync(items_[q], items_host_[q].data(), sizeof(BatchItem) * cnt, cudaMemcpyHostToDevice,
-                               s_));
-    count_host_[q] = cnt;
+    for (int l = 0; l < kLists; ++l) list_host_[l][q].clear();
+    for (const BatchItem& w : items_host_[q]) {
+      const int t = w.row0 / kTile;
+      list_host_[kListAll][q].push_back(w);
+      if (t % 2 == 0) list_host_[kListRpt2][q].push_back(w);
+      if (t % 4 == 0) list_host_[kListRpt4][q].push_back(w);
+      if (w.chunk == 0) list_host_[kListTrue][q].push_back(w);
+    }
+    for (int l = 0; l < kLists; ++l) {
+      const int cnt = (int)list_host_[l][q].size();
+      if (cnt)
+        MGB_CUDA(cudaMemcpyAsync(items_[l][q], list_host_[l][q].data(), sizeof(BatchItem) * cnt,
+                                 cudaMemcpyHostToDevice, s_));
+      count_host_[l][q] = cnt;
+    }
   }
   for (int q = 0; q < kClasses; ++q) has_mixed_[q] = has_fp64_[q] = false;
   for (int i = 0; i < nslots_; ++i) {
-    if (!host_[i].in_use) continue;
+    if (!host_[i].in_use || !listed_[i]) continue;
     const int cls = class_of(host_[i].dim, host_[i].R);
     (host_[i].precision == MGB_PREC_MIXED ? has_mixed_ : has_fp64_)[cls] = true;
   }
@@ -845,19 +903,21 @@ int BatchEngine::sync_items() {
   if (vcount_host_)
     MGB_CUDA(cudaMemcpyAsync(vitems_, vitems_host_.data(), sizeof(VecItem) * vcount_host_, cudaMemcpyHostToDevice,
                              s_));
-  MGB_CUDA(cudaMemcpyAsync(counters_ + kOffCount, count_host_, sizeof(int) * kClasses, cudaMemcpyHostToDevice, s_));
+  MGB_CUDA(cudaMemcpyAsync(counters_ + kOffCount, count_host_, sizeof(int) * kLists * kClasses,
+                           cudaMemcpyHostToDevice, s_));
   MGB_CUDA(cudaMemcpyAsync(counters_ + kOffVecCount, &vcount_host_, sizeof(int), cudaMemcpyHostToDevice, s_));
   MGB_CUDA(cudaStreamSynchronize(s_));
   items_dirty_ = false;
   return MGB_OK;
 }
 
-// Matvec queue of class `cls` and mode: (claim, finished) counters at
-// kOffMv + (cls * 3 + mode) * 2, item count at kOffCount + cls.
-static WorkQueue make_queue(const BatchItem* items, int* counters, int cls, int mode) {
+// Matvec queue of class `cls` and mode over item list `list`: (claim,
+// finished) counters at kOffMv + (cls * 3 + mode) * 2, item count at
+// kOffCount + list * kClasses + cls.
+static WorkQueue make_queue(const BatchItem* items, int* counters, int cls, int mode, int list) {
   WorkQueue q;
   q.items = items;
-  q.count = counters + BatchEngine::kOffCount + cls;
+  q.count = counters + BatchEngine::kOffCount + list * BatchEngine::kClasses + cls;
   q.counter = counters + BatchEngine::kOffMv + (cls * 3 + mode) * 2;
   q.finished = reinterpret_cast<unsigned int*>(q.counter + 1);
   return q;
@@ -870,7 +930,8 @@ static void launch_mv32(const WorkQueue& q, const BatchSys* sys, int rpt, int gr
 }
 
 int BatchEngine::enqueue_mv32(int cls, int rpt, cudaStream_t s) {
-  const WorkQueue q = make_queue(items_[cls], counters_, cls, Q_MV32);
+  const int list = rpt == 4 ? kListRpt4 : kListRpt2;
+  const WorkQueue q = make_queue(items_[list][cls], counters_, cls, Q_MV32, list);
   const int grid = 4 * c_->num_sms;
   switch (cls) {
     case 0: launch_mv32<2, 1>(q, dev_sys_, rpt, grid, s); break;
@@ -895,7 +956,8 @@ static void launch_mv64(const WorkQueue& q, const BatchSys* sys, bool true_res, 
 }
 
 int BatchEngine::enqueue_mv64(int cls, int mode, cudaStream_t s) {
-  const WorkQueue q = make_queue(items_[cls], counters_, cls, mode);
+  const int list = mode == Q_MV64_TRUE ? kListTrue : kListAll;
+  const WorkQueue q = make_queue(items_[list][cls], counters_, cls, mode, list);
   const int grid = 2 * c_->num_sms;
   const double* t = c_->exp_table;
   const bool tr = mode == Q_MV64_TRUE;
@@ -988,7 +1050,7 @@ int BatchEngine::autotune() {
   MGB_CUDA(cudaEventCreate(&e1));
   int st = MGB_OK;
   for (int cls = 0; cls < kClasses && st == MGB_OK; ++cls) {
-    if (!count_host_[cls] || rpt_[cls]) continue;
+    if (!count_host_[kListAll][cls] || rpt_[cls]) continue;
     bool mixed = false;
     for (const BatchItem& w : items_host_[cls]) mixed |= host_[w.sys].precision == MGB_PREC_MIXED;
     if (!mixed) continue;
@@ -1023,41 +1085,48 @@ int BatchEngine::autotune() {
   return st;
 }
 
-int BatchEngine::run_steps(int steps, int* active_out) {
-  MGB_TRY(sync_items());
-  MGB_TRY(autotune());
-  // (re)capture when the set of non-empty classes, the slot range or a
-  // tuning choice changed
+// (Re)captures the step graph when the set of non-empty classes, the slot
+// range or a tuning choice changed.
+int BatchEngine::prepare_graph() {
   unsigned int sig = 0;
   for (int q = 0; q < kClasses; ++q) sig |= (has_mixed_[q] ? 1u : 0u) << q | (has_fp64_[q] ? 1u : 0u) << (q + 8);
   sig = sig * 31u + (unsigned)nslots_;
   for (int q = 0; q < kClasses; ++q) sig = sig * 31u + (unsigned)rpt_[q];
-  if (!graph_exec_ || sig != graph_sig_) {
-    if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
-    if (graph_) cudaGraphDestroy(graph_);
-    graph_exec_ = nullptr;
-    graph_ = nullptr;
-    MGB_CUDA(cudaStreamBeginCapture(s_, cudaStreamCaptureModeThreadLocal));
-    begin_capture_count();
-    int st = MGB_OK;
-    for (int i = 0; i < kStepsPerGraph && st == MGB_OK; ++i) st = enqueue_step();
-    graph_kernels_ = end_capture_count();
-    cudaError_t e = cudaStreamEndCapture(s_, &graph_);
-    if (st != MGB_OK) return st;
-    if (e != cudaSuccess) return cuda_error(e, "cudaStreamEndCapture", __FILE__, __LINE__);
-    MGB_CUDA(cudaGraphInstantiate(&graph_exec_, graph_, 0));
-    graph_sig_ = sig;
-  }
+  if (graph_exec_ && sig == graph_sig_) return MGB_OK;
+  if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+  if (graph_) cudaGraphDestroy(graph_);
+  graph_exec_ = nullptr;
+  graph_ = nullptr;
+  MGB_CUDA(cudaStreamBeginCapture(s_, cudaStreamCaptureModeThreadLocal));
+  begin_capture_count();
+  int st = MGB_OK;
+  for (int i = 0; i < kStepsPerGraph && st == MGB_OK; ++i) st = enqueue_step();
+  graph_kernels_ = end_capture_count();
+  cudaError_t e = cudaStreamEndCapture(s_, &graph_);
+  if (st != MGB_OK) return st;
+  if (e != cudaSuccess) return cuda_error(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+  MGB_CUDA(cudaGraphInstantiate(&graph_exec_, graph_, 0));
+  graph_sig_ = sig;
+  return MGB_OK;
+}
+
+int BatchEngine::run_steps(int steps, int* active_out) {
+  MGB_TRY(sync_items());
+  MGB_TRY(autotune());
   int done_steps = 0;
-  int active = 0;
-  for (int i = 0; i < nslots_; ++i) active += host_[i].in_use;
+  int active = listed_count_;
   while (active > 0 && done_steps < steps) {
+    MGB_TRY(prepare_graph());
     MGB_CUDA(cudaGraphLaunch(graph_exec_, s_));
     count_launches(graph_kernels_);
     done_steps += kStepsPerGraph;
     MGB_CUDA(cudaMemcpyAsync(active_host_, counters_ + kOffActive, sizeof(int), cudaMemcpyDeviceToHost, s_));
     MGB_CUDA(cudaStreamSynchronize(s_));
     active = *active_host_;
+    if (active < listed_count_) {  // systems finished in this replay
+      MGB_TRY(prune_finished());
+      MGB_TRY(sync_items());
+    }
   }
   if (active_out) *active_out = active;
   return MGB_OK;

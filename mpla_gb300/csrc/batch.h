@@ -63,13 +63,18 @@ class BatchEngine {
   static constexpr int kClasses = 8;        // (dim 2|3) x (R 1|2|4|8)
   static constexpr int kStepsPerGraph = 8;  // CG iterations per graph replay
   static constexpr int kBranches = 2 * kClasses;  // concurrent matvec launches of a phase
+  // Matvec item lists per class: every item (FP64 matvecs), the items whose
+  // row tile is even / a multiple of 4 (FP32 variants with 2 / 4 rows per
+  // thread cover 2 / 4 consecutive row tiles), the chunk-0 items (whole-row
+  // true residuals).
+  static constexpr int kListAll = 0, kListRpt2 = 1, kListRpt4 = 2, kListTrue = 3, kLists = 4;
   // device counters: matvec queues (claim, finished) per class and mode,
-  // item counts per class, the active-system count, vector-phase queues
-  // (claim, finished) per phase and the vector item count
+  // item counts per list and class, the active-system count, vector-phase
+  // queues (claim, finished) per phase and the vector item count
   static constexpr int kOffMv = 0;
   static constexpr int kOffCount = 6 * kClasses;
-  static constexpr int kOffActive = 7 * kClasses;
-  static constexpr int kOffVec = 7 * kClasses + 1;
+  static constexpr int kOffActive = kOffCount + kLists * kClasses;
+  static constexpr int kOffVec = kOffActive + 1;
   static constexpr int kOffVecCount = kOffVec + 8;
   static constexpr int kCounterInts = kOffVecCount + 4;
 
@@ -85,8 +90,12 @@ class BatchEngine {
 
  private:
   static int class_of(int dim, int R);
+  long long list_capacity(int l) const { return l == kListAll ? max_items_ : max_items_ / 2; }
   static size_t bytes_needed(int n, int dim, int nrhs, int precision);
   void release_slot(int slot);
+  void unlist(const std::vector<char>& drop);
+  int prune_finished();
+  int prepare_graph();
   int sync_items();
   int autotune();
   int enqueue_step();
@@ -103,9 +112,12 @@ class BatchEngine {
   std::vector<BatchSys> host_;
   std::vector<void*> blocks_;
   BatchSys* dev_sys_ = nullptr;
-  BatchItem* items_[kClasses] = {};
-  std::vector<BatchItem> items_host_[kClasses];
-  int count_host_[kClasses] = {};
+  BatchItem* items_[kLists][kClasses] = {};
+  std::vector<BatchItem> items_host_[kClasses];  // every item; the other lists are derived
+  std::vector<BatchItem> list_host_[kLists][kClasses];
+  int count_host_[kLists][kClasses] = {};
+  std::vector<char> listed_;  // slot's items are in the lists (admitted and not seen finished)
+  int listed_count_ = 0;
   bool has_mixed_[kClasses] = {};  // classes holding mixed / FP64 systems
   bool has_fp64_[kClasses] = {};
   VecItem* vitems_ = nullptr;
