@@ -293,6 +293,12 @@ __global__ void __launch_bounds__(kTile) k_bmv64(WorkQueue q, const BatchSys* __
     const int n = S.n;
     const double* v = TRUE_RES ? S.x : S.d;
     const int i = w.row0 + threadIdx.x;
+    // true residuals only for the lanes whose replacement is due (the
+    // others, and padding lanes, would cost 8 FP64 operations per entry for
+    // a z that nothing reads); the same for every thread, so no divergence
+    bool on[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) on[k] = !TRUE_RES || (S.lanes[k].done == LANE_RUNNING && S.lanes[k].flag);
     const int c0 = TRUE_RES ? 0 : w.chunk * kChunkCols;
     const int c1 = TRUE_RES ? n : min(n, c0 + kChunkCols);
     double pi[DIM];
@@ -327,8 +333,10 @@ __global__ void __launch_bounds__(kTile) k_bmv64(WorkQueue q, const BatchSys* __
         for (int k = 0; k < R; ++k) {
           const double vk = sv[t * R + k];
           if (TRUE_RES) {
-            const double p = __dmul_rn(e, vk);
-            dd_add(acc[k], cmp[k], p, fma(e, vk, -p));
+            if (on[k]) {
+              const double p = __dmul_rn(e, vk);
+              dd_add(acc[k], cmp[k], p, fma(e, vk, -p));
+            }
           } else {
             tile[k] = fma(e, vk, tile[k]);
           }
@@ -343,6 +351,7 @@ __global__ void __launch_bounds__(kTile) k_bmv64(WorkQueue q, const BatchSys* __
       for (int k = 0; k < R; ++k) {
         const long long o = (long long)i * R + k;
         if (TRUE_RES) {
+          if (!on[k]) continue;
           const double p = __dmul_rn(S.nugget, v[o]);
           dd_add(acc[k], cmp[k], p, fma(S.nugget, v[o], -p));
           // b and acc agree to a few digits, so b - acc is (nearly) exact

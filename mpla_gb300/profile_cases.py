@@ -9,6 +9,7 @@ that ends by itself (a few hundred MB on the device at most):
   python -m mpla_gb300.profile_cases mixed_cg    # 300 mixed-CG iterations, n = 16384, d = 2
   python -m mpla_gb300.profile_cases batch       # 100 steps of a 24-system batch (n <= 4096)
   python -m mpla_gb300.profile_cases batch128    # 16 timed steps of 128 batch systems (n <= 16384)
+  python -m mpla_gb300.profile_cases batch128_solve  # the same 128 systems solved to 1e-10
   python -m mpla_gb300.profile_cases mixed_c3    # full mixed solve, n = 131072, d = 3, l = 0.08
   python -m mpla_gb300.profile_cases all
 
@@ -101,6 +102,35 @@ def case_batch128(steps=16):
     batch.close()
 
 
+def case_batch128_solve():
+    """The same 128 systems run to relres 1e-10: wall time, and per system
+    (slowest ten) the iterations and FP64 true residuals of its slowest
+    right-hand side."""
+    import time
+
+    spec = synth.batch_spec(512)
+    batch = mg.Batch(128)
+    handles = []
+    for k in range(128):
+        g = synth.batch_system(spec, k)
+        handles.append((k, batch.add(g.scaled(), g.nugget, g.b, precision=mg.PREC_MIXED)))
+    t0 = time.perf_counter()
+    active = batch.run()
+    sec = time.perf_counter() - t0
+    rows = []
+    for k, h in handles:
+        n, r = int(spec.n[k]), int(spec.nrhs[k])
+        _, infos = batch.result(h, n, r)
+        rows.append((max(i.iterations for i in infos), max(i.fp64_matvecs for i in infos),
+                      sum(i.fp64_matvecs for i in infos), n, int(spec.dim[k]), float(spec.ell[k]), r))
+    rows.sort(reverse=True)
+    print(f"batch128_solve: {sec:.2f} s, {active} unfinished, {sum(x[2] for x in rows)} FP64 true residuals "
+          f"over all right-hand sides")
+    for it, rep, _, n, d, ell, r in rows[:10]:
+        print(f"  n={n} d={d} l={ell:.3f} nrhs={r}: {it} iterations, {rep} FP64 true residuals")
+    batch.close()
+
+
 def case_mixed_c3():
     """The mixed-precision configuration: n = 131072 points U[0,1]^3, l = 0.08,
     nugget 1e-4, b = sin(2 pi x1) cos(2 pi x2), solved to relres 1e-10."""
@@ -124,12 +154,14 @@ def case_mixed_c3():
 
 
 CASES = {"dgemv": case_dgemv, "gauss_f64": case_gauss_f64, "gauss_mixed": case_gauss_mixed,
-         "mixed_cg": case_mixed_cg, "batch": case_batch, "batch128": case_batch128, "mixed_c3": case_mixed_c3}
+         "mixed_cg": case_mixed_cg, "batch": case_batch, "batch128": case_batch128,
+         "batch128_solve": case_batch128_solve, "mixed_c3": case_mixed_c3}
 
 
 def main(argv):
     mg.init(0)
-    names = [k for k in CASES if k not in ("mixed_c3", "batch128")] if (not argv or argv[0] == "all") else argv
+    long_cases = ("mixed_c3", "batch128", "batch128_solve")
+    names = [k for k in CASES if k not in long_cases] if (not argv or argv[0] == "all") else argv
     for name in names:
         CASES[name]()
     mg.synchronize()
