@@ -21,8 +21,8 @@
 //           stop test, and for mixed lanes whether the FP64 true residual is
 //           due
 //   mv64r   (system, 128 rows) items of mixed systems with a pending
-//           replacement: z = b - K x, FP64 entries, products and sums in
-//           double-double
+//           replacement: z = b - K x for the lanes that are due, FP64
+//           entries, products and sums in double-double
 //   replace r = z for those lanes, convergence test on the FP64 true
 //           residual, restart of the direction
 //   dir     d = beta d + r (and its FP32 copy)
