@@ -4,7 +4,7 @@ ctypes binding of ``mpla_oracle.c`` (an FP64 restatement of the reference
 algorithms: dgemv, ddot, the Gaussian kernel entries and matvec, CG with both
 stopping rules, BiCGSTAB, the erf right-hand side, the vector file format).
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use
-it, and only as the checker.
+it, and only to check results against.
 """
 from __future__ import annotations
 

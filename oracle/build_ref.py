@@ -1,15 +1,16 @@
-"""Builds the reference MPLA as a checker: oracle/_ref/libmplaref.so.
+"""Builds the reference MPLA for parity checks: oracle/_ref/libmplaref.so.
 
 TEST INFRASTRUCTURE.  The reference's hot-path sources are compiled as they
 are (no edit) with a single-rank MPI stand-in (oracle/ref_mpi/mpi.h) and our
 harness (oracle/ref_harness.cu), which drives them through their public API.
 
 Steps
-  1. stage: where the reference tree is present (this build container), copy
-     the nine source files of the path into oracle/_ref/src/.  That folder is
-     git-ignored (never committed) but travels with the working tree to the
-     GPU machine, which is an AArch64 machine where an x86 build cannot run and
-     where the reference tree is absent, so the sources are compiled there.
+  1. stage: where the reference tree is present (the x86 development
+     machine), copy the nine source files of the path into oracle/_ref/src/.
+     That folder is git-ignored (never committed) but travels with the
+     working tree to the AArch64 machine that runs the GPU work, where an x86
+     build cannot run and the reference tree is absent, so the sources are
+     compiled there.
   2. compile: g++ for mpla.cpp (host code), nvcc for the CUDA files
      (relocatable device code for the virtual system_assembler, device-linked
      like the reference's own Makefile:96-114), one -gencode for sm_103a.

@@ -2,7 +2,8 @@
  *
  * A plain-C, FP64 restatement of the reference algorithms on the hot path,
  * used by tests/, by __graft_entry__.smoke() and by bench.py's CPU-baseline
- * leg as the checker.  The product never links, loads or calls this code.
+ * leg, to check results against.  The product never links, loads or calls
+ * this code.
  *
  * Every function names the reference code it restates (paths inside the
  * MPLA source tree).  Floating-point contraction is disabled at build time
@@ -327,7 +328,7 @@ double orc_true_relres_accurate(const orc_operator* op, const double* b, const d
   return sqrt(rr) / sqrt(bb);
 }
 
-/* Operator matvec exposed for the checker. */
+/* Operator matvec exposed for the tests. */
 void orc_apply(const orc_operator* op, const double* x, double* y) { mv(op, x, y); }
 
 /* File format of mpla_save_vector (src/mpla.cpp:605-652): int32 n followed by
