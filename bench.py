@@ -48,9 +48,10 @@ L2_FLUSH_BYTES = 512 << 20
 # reference iterations into solves/s.  Other sizes fall back to the mixed
 # count (a lower bound on the FP64 count for this family).
 FP64_ITERATIONS_N65536 = 18958
-# DRAM bytes (read + write) of one launch of the FP32 group kernel at
-# n = 65536, d = 2 from an ncu capture (profiles/gauss_f32_group_n65536_d2.md):
-# points, slots and x stay in L2
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
+# the FP32 group kernel at n = 65536, d = 2, from one ncu capture of that
+# launch (points, slots and x stay in L2).  Not measured per run: ncu is not
+# run inside the benchmark.
 GROUP_KERNEL_DRAM_BYTES_N65536 = 1.462272e6 + 0.571648e6
 SFU_EX2_PER_CLK_SM = 32.0
 SMI_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -498,7 +499,8 @@ def run_ours(args, world, rank, local):
                      "achieved": mixed_rate / 1e12, "peak": sfu_peak / 1e12, "unit": "Tex2/s",
                      "frac": mixed_rate / sfu_peak,
                      "traffic": GROUP_KERNEL_DRAM_BYTES_N65536 if (n == N_FULL and DIM == 2) else None,
-                     "traffic_unit": "DRAM bytes per launch (ncu)",
+                     "traffic_unit": "DRAM bytes per launch",
+                     "traffic_source": "one ncu capture of this kernel at n=65536, d=2 (not measured in this run)",
                      "per_unit": "1 evaluated kernel entry = 1 ex2 (+ ~7 FP32 issue slots); each unordered pair of "
                                  "points evaluated once, tile pairs below 2^-40 skipped",
                      "evaluated_per_launch": evaluated, "algorithmic_entries_per_launch": entries,
@@ -514,52 +516,77 @@ def run_ours(args, world, rank, local):
 
 
 # ---------------------------------------------------------- reference arm
+def reference_dense(ref, n: int = 4096, reps: int = 10) -> dict:
+    """C1 on the reference: mpla_dgemv (cuBLAS Dgemv inside, mpla.cpp:716-751)
+    and the dense CG of mpla_generic_conjugate_gradient_with_checkpoint_restart
+    with the cuBLAS user core of the reference's test_cg.cpp:38-43."""
+    from mpla_gb300 import synth
+
+    A, b, x0 = synth.config_dense(0)
+    _, gemv_ms = ref.dgemv(A, np.linspace(-1.0, 1.0, n), reps=50)
+    for _ in range(2):
+        ref.solve_dense(A, b, x0, 1000, EPS, ref.SOLVER_CG_REL)
+    times, mvs = [], []
+    for _ in range(reps):
+        _, mv, ms = ref.solve_dense(A, b, x0, 1000, EPS, ref.SOLVER_CG_REL)
+        times.append(ms)
+        mvs.append(mv)
+    solve_ms = float(np.median(times))
+    gemv_bytes = 8.0 * n * n + 16.0 * n
+    return {"workload": "dense FP64 CG, n=4096, A = M^T M/n + I (M ~ U[-1,1], seed 0), b = 1, relres 1e-10",
+            "solves_per_s": 1e3 / solve_ms, "ms_per_solve": solve_ms,
+            "iterations": ref.iterations(ref.SOLVER_CG_REL, mvs[-1]),
+            "dgemv": {"ms": gemv_ms, "achieved_gbs": gemv_bytes / (gemv_ms * 1e-3) / 1e9, "bytes": gemv_bytes,
+                      "what": "mpla_dgemv (cuBLAS Dgemv plus the reference's per-call allocations and copies)"}}
+
+
 def run_reference(args, world, rank, local):
     if rank != 0:
         return
+    sys.path.insert(0, str(ROOT / "oracle"))
     refdir = ROOT / "oracle" / "_ref"
     lib = refdir / "libmplaref.so"
     if not lib.exists():
         try:
-            sys.path.insert(0, str(ROOT / "oracle"))
             import build_ref
 
             build_ref.build()
         except Exception as e:  # noqa: BLE001
             print(json.dumps({"impl": "reference", "unavailable": f"reference MPLA not built: {e}"}))
             return
-    import ctypes as C
-
+    from oracle import reference as ref
     from mpla_gb300 import synth
 
-    L = C.CDLL(str(lib))
-    L.ref_init.argtypes = [C.c_int]
-    L.ref_cg_gauss_sample.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_double, C.c_void_p, C.c_int, C.c_double,
-                                      C.POINTER(C.c_double), C.POINTER(C.c_int)]
-    L.ref_cg_gauss_sample.restype = C.c_int
-    if L.ref_init(local) != 0:
-        print(json.dumps({"impl": "reference", "unavailable": "reference MPLA failed to initialise the device"}))
+    try:
+        ref.lib(local)
+    except RuntimeError as e:
+        print(json.dumps({"impl": "reference", "unavailable": str(e)}))
         return
+    L = ref.lib(local)
+    import ctypes as C
+
     n = args.n
     prob = synth.gauss_problem(n, DIM, ELL, NUGGET, seed=0)
     pts = np.ascontiguousarray(prob.scaled())
     b = np.ascontiguousarray(prob.b)
     sample_iters = args.ref_sample_iters
     ms = C.c_double()
-    it = C.c_int()
+    mv = C.c_int()
     for _ in range(args.warmup):
         L.ref_cg_gauss_sample(n, DIM, pts.ctypes.data, NUGGET, b.ctypes.data, sample_iters, EPS, C.byref(ms),
-                              C.byref(it))
-    total_ms, total_it = 0.0, 0
+                              C.byref(mv))
+    total_ms, total_mv = 0.0, 0
     for _ in range(args.steps):
         st = L.ref_cg_gauss_sample(n, DIM, pts.ctypes.data, NUGGET, b.ctypes.data, sample_iters, EPS, C.byref(ms),
-                                   C.byref(it))
+                                   C.byref(mv))
         if st != 0:
             print(json.dumps({"impl": "reference", "unavailable": f"reference CG sample failed (status {st})"}))
             return
         total_ms += ms.value
-        total_it += it.value
-    ms_per_iter = total_ms / max(1, total_it)
+        total_mv += mv.value
+    # every matvec of the sample is inside the timed call: the r0 matvec and
+    # one per iteration, so the time per iteration is the time per matvec
+    ms_per_iter = total_ms / max(1, total_mv)
     iters_fp64 = fp64_iterations(args, 0)
     value = (1.0 / (ms_per_iter * 1e-3 * iters_fp64)) if iters_fp64 else None
     line = {
@@ -571,12 +598,15 @@ def run_reference(args, world, rank, local):
                    "solver": "reference MPLA FP64 CG (mpla_generic_conjugate_gradient_with_checkpoint_restart, "
                              "gaussian system_assembler, streamed cuBLAS core)"},
         "ms_per_iteration": ms_per_iter,
+        "sample_matvecs": total_mv,
         "iterations_assumed": iters_fp64,
-        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": 1, "kind": "reference",
-                         "sample": f"{sample_iters} CG iterations per step of the reference MPLA built from its "
-                                   f"sources (GPU path, 1 rank), scaled by the FP64 iteration count"},
+        "extrapolation": f"each step runs {sample_iters} CG iterations ({sample_iters + 1} matvecs, all timed) of the "
+                         f"reference MPLA built from its sources (GPU, 1 rank); solves/s = 1 / (ms per matvec x "
+                         f"{iters_fp64} iterations, this library's FP64 CG count on the same system)",
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if not args.no_dense:
+        line["dense"] = reference_dense(ref)
     print(json.dumps(line), flush=True)
 
 

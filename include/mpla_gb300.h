@@ -47,7 +47,7 @@ extern "C" {
 
 /* inner matvec precision of the Gaussian solvers */
 #define MGB_PREC_FP64 0   /* plain FP64 CG */
-#define MGB_PREC_MIXED 1  /* FP32 matvec (split-BF16 tensor-core distances), FP64 vectors, dots, scalars and true residuals */
+#define MGB_PREC_MIXED 1  /* FP32 matvec (kernel chosen by mgb_set_mixed_matvec), FP64 vectors, dots, scalars and true residuals */
 
 /* ---------------------------------------------------------------- runtime */
 int mgb_version(void);
@@ -73,21 +73,26 @@ int mgb_host_free(void* ptr_host);
  * (mpla.cpp:716-751) at the 1x1 process grid. */
 int mgb_dgemv(int m, int n, const double* A_dev, int lda, const double* x_dev, double* y_dev, void* stream);
 /* y = A x like mgb_dgemv, for callers that cannot allocate device memory.
- * No counterpart in the reference.  Callers such as code running inside a
- * CUDA stream capture, plugins whose host framework owns every device
- * allocation, or latency-critical paths that must not take the allocator's
- * implicit synchronisation cannot call cudaMalloc; this entry point calls no
- * cudaMalloc, cudaFree or allocating library routine and never creates the
- * library context.  Its scratch (split-K partials and arrival counters) is a
- * fixed 8.1 MiB device array that every GPU loading the library holds until
- * the process exits.  Limits: m <= 1,048,512 rows (16383 strips of 64; half
- * that when lda is odd or A is not 16-byte aligned) and
- * m * ceil(n / 4096) <= 1,048,576; larger sizes return MGB_ERR_ARG.
- * All calls share that array: calls that overlap on the GPU (different
- * streams, or several host threads) race and must be serialised by the
- * caller.  The first call on a device resolves the array's device address
- * (cudaGetSymbolAddress with that device current), so make that first call
- * before any stream capture.  NULL `stream` is the legacy default stream. */
+ * No counterpart in the reference.  Some hosts of this code may not call
+ * cudaMalloc: plugins whose host framework owns every device allocation
+ * (its pool must account for all memory), and latency-critical paths that
+ * cannot take the allocator's implicit device synchronisation.  This entry
+ * point calls no cudaMalloc, cudaFree or allocating library routine and
+ * never creates the library context.  Its scratch (split-K partials and
+ * arrival counters) is a fixed 8.1 MiB device array that every GPU loading
+ * the library holds until the process exits.  Limits: m <= 1,048,512 rows
+ * (16383 strips of 64; half that when lda is odd or A is not 16-byte
+ * aligned) and m * ceil(n / 4096) <= 1,048,576; larger sizes return
+ * MGB_ERR_ARG with a message naming the limit.
+ * All calls share that array and it keeps the last call's contents (each
+ * call clears the counters it uses): calls that overlap on the GPU
+ * (different streams, or several host threads) race and must be serialised
+ * by the caller.  The first call on a device resolves the array's device
+ * address (cudaGetSymbolAddress with that device current); make that first
+ * call before any stream capture.  `stream` must belong to the current
+ * device (MGB_ERR_ARG otherwise); NULL is the legacy default stream.
+ * This variant stages x with plain loads and has no device-side wait, so it
+ * has no timeout to report: MGB_OK means the work was enqueued. */
 int mgb_dgemv_noalloc(int m, int n, const double* A_dev, int lda, const double* x_dev, double* y_dev,
                       void* stream);
 /* *result_host = <x, y>.  Replaces mpla_ddot (mpla.cpp:753-770). */
@@ -105,9 +110,11 @@ int mgb_daxpy(int n, double alpha, const double* x_dev, double* y_dev, void* str
 int mgb_gauss_matvec_f64(int rows, int cols, int row_offset, int col_offset, int dim,
                          const double* const* coords_dev, double nugget, int nugget_rule,
                          const double* x_dev, double* y_dev, void* stream);
-/* Same product with the mixed-precision kernel: FP32 arithmetic, squared
- * distances from split-BF16 tensor-core cross terms, exponentials on the SFU.
- * x and y stay FP64.  Square systems only (rows == cols, offsets 0). */
+/* Same product with the mixed-precision kernel chosen by
+ * mgb_set_mixed_matvec: FP32 arithmetic (by default squared distances from
+ * FP32 coordinate differences; MGB_MIXED_TENSOR forms them on the tensor
+ * cores), exponentials on the SFU.  x and y stay FP64.  Square systems only
+ * (rows == cols, offsets 0). */
 int mgb_gauss_matvec_mixed(int n, int dim, const double* const* coords_dev, double nugget,
                            const double* x_dev, double* y_dev, void* stream);
 /* Evaluate single entries K(i,j), 0 <= i,j < n, with the FP64 kernel's
@@ -156,7 +163,8 @@ int mgb_cg_gauss_host(int n, int dim, const double* coords_host, double nugget,
  * up after the call (no counterpart in the reference):
  *   MGB_MIXED_TENSOR  squared distances as a split-BF16 tcgen05 contraction,
  *                     exponentials on the SFU (sm_103a tensor cores);
- *   MGB_MIXED_SIMT    squared distances from FP32 coordinate differences.
+ *   MGB_MIXED_SIMT    squared distances from FP32 coordinate differences
+ *                     (the default).
  * Both are symmetric FP32 operators of the same kernel matrix. */
 #define MGB_MIXED_TENSOR 0
 #define MGB_MIXED_SIMT 1

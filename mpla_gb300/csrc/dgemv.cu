@@ -33,7 +33,9 @@ __device__ __forceinline__ double ld_stream1(const double* p) {
   return v;
 }
 
-template <int VEC>
+// BULK: stage x with one bulk copy and a bounded mbarrier wait (a wait that
+// gives up sets DEV_ERR_WAIT_TIMEOUT in *err); otherwise with plain loads.
+template <int VEC, bool BULK>
 __global__ void __launch_bounds__(kThreads) dgemv_kernel(int m, int n, const double* __restrict__ A,
                                                          long long lda, const double* __restrict__ x,
                                                          double* __restrict__ y, int cpw, int nsplit,
@@ -59,7 +61,7 @@ __global__ void __launch_bounds__(kThreads) dgemv_kernel(int m, int n, const dou
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
   // ---- stage x[col0 : col0+ncols) in shared memory
-  const bool use_bulk = ((reinterpret_cast<uintptr_t>(x + col0) & 15) == 0) && ((ncols & 1) == 0);
+  const bool use_bulk = BULK && ((reinterpret_cast<uintptr_t>(x + col0) & 15) == 0) && ((ncols & 1) == 0);
   if (use_bulk) {
     if (threadIdx.x == 0) {
       mbar_init(bar, 1);
@@ -183,11 +185,13 @@ int launch_dgemv(DeviceContext* c, int m, int n, const double* A, int lda, const
   const long long grid = (long long)strips * nsplit;
   if (grid > 0x7fffffffLL) return set_error(MGB_ERR_ARG, "dgemv: grid too large");
   if (vec2) {
-    dgemv_kernel<2><<<(unsigned)grid, kThreads, smem, s>>>(m, n, A, lda, x, y, cpw, nsplit,
-                                                         c->split_partials, c->tickets + 1, done, c->dev_error);
+    dgemv_kernel<2, true><<<(unsigned)grid, kThreads, smem, s>>>(m, n, A, lda, x, y, cpw, nsplit,
+                                                               c->split_partials, c->tickets + 1, done,
+                                                               c->dev_error);
   } else {
-    dgemv_kernel<1><<<(unsigned)grid, kThreads, smem, s>>>(m, n, A, lda, x, y, cpw, nsplit,
-                                                         c->split_partials, c->tickets + 1, done, c->dev_error);
+    dgemv_kernel<1, true><<<(unsigned)grid, kThreads, smem, s>>>(m, n, A, lda, x, y, cpw, nsplit,
+                                                               c->split_partials, c->tickets + 1, done,
+                                                               c->dev_error);
   }
   count_launches(1);
   MGB_CUDA(cudaGetLastError());
@@ -248,12 +252,18 @@ extern "C" int mgb_dgemv_noalloc(int m, int n, const double* A, int lda, const d
   int dev = 0;
   MGB_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) return set_error(MGB_ERR_ARG, "device index %d out of range", dev);
+  if (stream && s != cudaStreamLegacy && s != cudaStreamPerThread) {
+    // the scratch address below belongs to the current device
+    int sdev = -1;
+    MGB_CUDA(cudaStreamGetDevice(s, &sdev));
+    if (sdev != dev)
+      return set_error(MGB_ERR_ARG, "dgemv_noalloc: stream belongs to device %d, current device is %d", sdev, dev);
+  }
   unsigned char* scratch = nullptr;
   int sms = 0;
   MGB_TRY(noalloc_setup(dev, &scratch, &sms));
   double* partials = reinterpret_cast<double*>(scratch);
   unsigned int* tickets = reinterpret_cast<unsigned int*>(scratch + sizeof(double) * kNoAllocPartials);
-  unsigned int* err = tickets + kNoAllocTickets;
   // same column split as the allocating path, bounded by the fixed scratch
   int cpw = 128;
   const long long target = 6LL * sms;
@@ -268,12 +278,14 @@ extern "C" int mgb_dgemv_noalloc(int m, int n, const double* A, int lda, const d
   const size_t smem = 16 + sizeof(double) * (kWarps * cpw + kWarps * rows_per_strip);
   if (smem > 48 * 1024) return set_error(MGB_ERR_ARG, "dgemv_noalloc: column chunk too large");
   const long long grid = strips * nsplit;
+  // x is staged with plain loads: this variant has no device-side wait, so
+  // no error word exists that a caller would have to read back.
   if (vec2) {
-    dgemv_kernel<2><<<(unsigned)grid, kThreads, smem, s>>>(m, n, A, lda, x, y, cpw, nsplit, partials, tickets + 1,
-                                                         nullptr, err);
+    dgemv_kernel<2, false><<<(unsigned)grid, kThreads, smem, s>>>(m, n, A, lda, x, y, cpw, nsplit, partials,
+                                                                tickets + 1, nullptr, nullptr);
   } else {
-    dgemv_kernel<1><<<(unsigned)grid, kThreads, smem, s>>>(m, n, A, lda, x, y, cpw, nsplit, partials, tickets + 1,
-                                                         nullptr, err);
+    dgemv_kernel<1, false><<<(unsigned)grid, kThreads, smem, s>>>(m, n, A, lda, x, y, cpw, nsplit, partials,
+                                                                tickets + 1, nullptr, nullptr);
   }
   count_launches(1);
   MGB_CUDA(cudaGetLastError());

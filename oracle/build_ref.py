@@ -26,7 +26,9 @@ import subprocess
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-REF_TREE = Path("/root/reference/src")
+# Source tree of the reference (its src/ folder): MPLA_REFERENCE_SRC when set,
+# else where the development machine mounts it.  Only stage() reads it.
+REF_TREE = Path(os.environ.get("MPLA_REFERENCE_SRC", "/root/reference/src"))
 OUT = HERE / "_ref"
 SRC = OUT / "src"
 LIB = OUT / "libmplaref.so"
@@ -36,15 +38,18 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMPAT = ["-DcudaThreadSynchronize=cudaDeviceSynchronize", "-include", "stdio.h", "-include", "math.h"]
 
 
-def stage() -> bool:
-    if not REF_TREE.is_dir():
+def stage(ref_tree: Path | None = None) -> bool:
+    """Copies the path's sources from `ref_tree` (default REF_TREE) into
+    oracle/_ref/src; True when the staged sources are complete."""
+    tree = Path(ref_tree) if ref_tree else REF_TREE
+    if not tree.is_dir():
         return all((SRC / f).exists() for f in FILES)
     SRC.mkdir(parents=True, exist_ok=True)
     for f in FILES:
         dst = SRC / f
         if dst.exists():
             os.chmod(dst, 0o644)
-        shutil.copyfile(REF_TREE / f, dst)
+        shutil.copyfile(tree / f, dst)
         os.chmod(dst, 0o644)
     return True
 
@@ -55,8 +60,8 @@ def _run(cmd):
         raise RuntimeError(" ".join(cmd) + "\n" + res.stdout + res.stderr)
 
 
-def build() -> Path:
-    if not stage():
+def build(ref_tree: Path | None = None) -> Path:
+    if not stage(ref_tree):
         raise RuntimeError("reference sources not staged (oracle/_ref/src) and no reference tree to stage from")
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     cuda = Path(nvcc).resolve().parent.parent

@@ -320,13 +320,15 @@ int ref_solve_gauss(int n, int dim, const double* pts, double nugget, const doub
 }
 
 // Bounded sample for the benchmark: `iters` CG iterations (iter_max = iters+1)
-// of the relative-residual CG from x0 = 0; returns device ms and iterations run.
+// of the relative-residual CG from x0 = 0; returns the device ms of the
+// whole call and the number of matvecs it ran (the r0 matvec plus one per
+// iteration), so that the caller divides the time by the matvecs timed.
 int ref_cg_gauss_sample(int n, int dim, const double* pts, double nugget, const double* b, int iters, double eps,
-                        double* ms, int* iters_run) {
+                        double* ms, int* matvecs_run) {
   std::vector<double> x(n, 0.0);
   int mv = 0;
   const int st = ref_solve_gauss(n, dim, pts, nugget, b, x.data(), iters + 1, eps, 0, &mv, ms);
-  if (iters_run) *iters_run = mv - 1;
+  if (matvecs_run) *matvecs_run = mv;
   return st;
 }
 

@@ -3,23 +3,26 @@
 Each case launches one hot kernel a few times on inputs sized for a capture
 that ends by itself (a few hundred MB on the device at most):
 
-  python -m mpla_gb300.profile_cases dgemv       # dense dgemv, n = 4096 (134 MB matrix)
-  python -m mpla_gb300.profile_cases gauss_f64   # FP64 Gaussian matvec, n = 16384, d = 2
-  python -m mpla_gb300.profile_cases gauss_mixed # FP32/SFU Gaussian matvec, n = 65536, d = 2
-  python -m mpla_gb300.profile_cases mixed_cg    # 300 mixed-CG iterations, n = 16384, d = 2
-  python -m mpla_gb300.profile_cases batch       # 100 steps of a 24-system batch (n <= 4096)
-  python -m mpla_gb300.profile_cases batch128    # 16 timed steps of 128 batch systems (n <= 16384)
-  python -m mpla_gb300.profile_cases batch128_solve  # the same 128 systems solved to 1e-10
-  python -m mpla_gb300.profile_cases mixed_c3    # full mixed solve, n = 131072, d = 3, l = 0.08
-  python -m mpla_gb300.profile_cases all
+  python profile_cases.py dgemv       # dense dgemv, n = 4096 (134 MB matrix)
+  python profile_cases.py gauss_f64   # FP64 Gaussian matvec, n = 16384, d = 2
+  python profile_cases.py gauss_mixed # FP32/SFU Gaussian matvec, n = 65536, d = 2
+  python profile_cases.py mixed_cg    # 300 mixed-CG iterations, n = 16384, d = 2
+  python profile_cases.py batch       # 100 steps of a 24-system batch (n <= 4096)
+  python profile_cases.py batch128    # 16 timed steps of 128 batch systems (n <= 16384)
+  python profile_cases.py batch128_solve  # the same 128 systems solved to 1e-10
+  python profile_cases.py mixed_c3    # full mixed solve, n = 131072, d = 3, l = 0.08
+  python profile_cases.py all
 
 Prints the CUDA-event time per launch of each case.
 """
 from __future__ import annotations
 
 import sys
+from pathlib import Path
 
 import numpy as np
+
+sys.path.insert(0, str(Path(__file__).resolve().parent))
 
 import mpla_gb300 as mg
 from mpla_gb300 import synth

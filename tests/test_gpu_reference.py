@@ -90,3 +90,24 @@ def test_bicgstab_matches_reference(gpu):
     assert info.status == 0
     assert abs(info.iterations - k_ref) <= max(2, int(0.2 * k_ref))
     assert np.allclose(dx.numpy(), x_ref, rtol=1e-8, atol=1e-10)
+
+
+# The benchmark families at n = 8192: the FP64 CG system of the n = 65536,
+# d = 2 configuration (l = 0.05) and the kernel of the n = 131072, d = 3
+# mixed configuration (l = 0.08), nugget 1e-4, b = sin(2 pi x1) cos(2 pi x2),
+# x0 = 0, relres 1e-10.  The reference runs to convergence (about 4.5 ms per
+# iteration on GB300); this library's FP64 count must fall within 3 % of it.
+@pytest.mark.parametrize("dim,ell", [(2, 0.05), (3, 0.08)])
+def test_gauss_cg_iterations_match_reference_n8192(gpu, dim, ell):
+    n = 8192
+    prob = synth.gauss_problem(n, dim, ell, 1e-4, seed=0)
+    pts, b = prob.scaled(), prob.b
+    x_ref, mv, ms = ref.solve_gauss(pts, 1e-4, b, np.zeros(n), 100000, 1e-10, ref.SOLVER_CG_REL)
+    k_ref = ref.iterations(ref.SOLVER_CG_REL, mv)
+    dp = gpu.GaussPoints(pts)
+    db, dx = gpu.DeviceArray.from_numpy(b), gpu.DeviceArray(n)
+    dx.zero()
+    info = gpu.cg_gauss(dp, 1e-4, db.ptr, dx.ptr, iter_max=100000, eps=1e-10)
+    print(f"n={n} d={dim} l={ell}: reference {k_ref} iterations ({ms / 1e3:.1f} s), this library {info.iterations}")
+    assert info.status == 0
+    assert abs(info.iterations - k_ref) <= 0.03 * k_ref, (info.iterations, k_ref)

@@ -1,12 +1,14 @@
-"""The allocation-free dgemv entry point against the regular one.
+"""The allocation-free dgemv entry point (mgb_dgemv_noalloc).
 
-mgb_dgemv_noalloc serves callers that cannot call cudaMalloc (code inside a
-stream capture, plugins whose host framework owns all device memory,
-latency-critical paths that must not synchronise on the allocator).  It
-keeps its scratch in a fixed device array shared by all calls, so the test
-makes two calls in a row for each shape and compares both with mgb_dgemv
-through the C ABI, at the 1e-13 relative bar of the dgemv tests.  This file
-is collected last so that a failure here does not hide the other results.
+Some callers of this library may not call cudaMalloc: plugins whose host
+framework owns every device allocation, and latency-critical paths that
+cannot take the allocator's implicit device synchronisation.  For them
+mgb_dgemv_noalloc keeps its scratch in a fixed device array shared by all
+calls.  The test makes two calls in a row for each shape (the second call
+sees the first call's leftovers in the array) and compares both with the
+FP64 oracle and with mgb_dgemv through the C ABI, at the 1e-13 relative bar
+of the dgemv tests.  This file is collected last so that a failure here does
+not hide the other results.
 """
 import ctypes as C
 
@@ -27,28 +29,31 @@ def _free_bytes():
 
 
 @pytest.mark.parametrize("m,n,lda,off", [(4096, 4096, None, 0), (1000, 777, None, 0), (513, 300, 515, 1),
-                                         (70000, 20, None, 0)])
-def test_noalloc_dgemv_matches_dgemv_twice(gpu, m, n, lda, off):
+                                         (70000, 20, None, 0), (64, 20000, None, 0)])
+def test_noalloc_dgemv_matches_oracle_and_dgemv_twice(gpu, orc, m, n, lda, off):
     rng = np.random.default_rng(m + n)
     lda = lda or m
     buf = np.zeros(off + lda * n)
-    A = rng.uniform(-1, 1, (m, n))
+    A = np.asfortranarray(rng.uniform(-1, 1, (m, n)))
     for j in range(n):
         buf[off + j * lda: off + j * lda + m] = A[:, j]
     dA = gpu.DeviceArray.from_numpy(buf)
     a_ptr = dA.ptr + 8 * off
     L = gpu.lib()
-    scale = np.abs(A) @ np.ones(n)
     for call in range(2):
         x = rng.uniform(-1, 1, n)
+        scale = np.abs(A) @ np.abs(x)
         dx = gpu.DeviceArray.from_numpy(x)
         y_ref, y_na = gpu.DeviceArray(m), gpu.DeviceArray(m)
+        y_na.upload(np.full(m, np.nan))  # stale output must be overwritten
         gpu.check(L.mgb_dgemv(m, n, a_ptr, lda, dx.ptr, y_ref.ptr, None))
         gpu.synchronize()
         gpu.check(L.mgb_dgemv_noalloc(m, n, a_ptr, lda, dx.ptr, y_na.ptr, None))
         gpu.synchronize()
-        got, want = y_na.numpy(), y_ref.numpy()
-        assert np.max(np.abs(got - want) / (scale * np.max(np.abs(x)))) <= TOL, (call, m, n)
+        got = y_na.numpy()
+        want = orc.dgemv(A, x)
+        assert np.max(np.abs(got - want) / scale) <= TOL, ("oracle", call, m, n)
+        assert np.max(np.abs(got - y_ref.numpy()) / scale) <= TOL, ("mgb_dgemv", call, m, n)
 
 
 def test_noalloc_dgemv_allocates_nothing(gpu):
@@ -76,3 +81,4 @@ def test_noalloc_dgemv_rejects_sizes_beyond_its_scratch(gpu):
     assert b"exceeds" in L.mgb_last_error()
     st = L.mgb_dgemv_noalloc(2_000_000, 2, d.ptr, 2_000_000, d.ptr, d.ptr, None)
     assert st == gpu.MGB_ERR_ARG
+    assert b"exceeds" in L.mgb_last_error()
