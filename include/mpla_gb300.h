@@ -217,6 +217,37 @@ int mgb_batch_result(mgb_batch* b, int handle, double* x_host, mgb_solve_info* i
 int mgb_batch_tuning(mgb_batch* b, int* rows_per_thread, float* ms);
 int mgb_batch_destroy(mgb_batch* b);
 
+/* ------------------------------------ device-linked generic assemblers */
+/* A user subclass of system_assembler (system_assembler.h) lives in the
+ * device code of the user's own module, so only a kernel device-linked into
+ * that module can call its virtual get_matrix_entry / get_rhs_entry -- the
+ * constraint of MPLA's own build, which device-links
+ * generic_system_adapter.o with the user's objects (src/Makefile:96-114).
+ * lib/mpla_generic_device.o (relocatable device code, built with libmpla.so)
+ * holds those kernels; linked into the user's module with -rdc it registers
+ * them here from a static constructor, and the generic_system_adapter.h
+ * cores and the solvers then evaluate user assemblers with them.  Factory
+ * Gaussian assemblers never need it.  Callers do not use this directly. */
+#define MGB_GENERIC_DEVICE_ABI 1
+typedef struct mgb_generic_device_code {
+  int abi_version; /* MGB_GENERIC_DEVICE_ABI */
+  /* y[i] = sum_{j < cols} K(row_offset + i, col_offset + j) x[j], i < rows;
+   * columns split in nsplit ranges of cols_per_split, partials (nsplit x rows)
+   * and tickets (one per 128-row tile, zero on entry and on exit) reduced in
+   * a fixed order; the launch returns at once when *skip_dev != 0.
+   * Returns a cudaError_t value. */
+  int (*matvec)(const void* assembler_dev, int rows, int cols, int row_offset, int col_offset,
+                const double* x_dev, double* y_dev, int cols_per_split, int nsplit, double* partials_dev,
+                unsigned int* tickets_dev, const int* skip_dev, void* stream);
+  /* b[i] = get_rhs_entry(row_offset + i), i < rows.  Returns a cudaError_t. */
+  int (*rhs)(const void* assembler_dev, int rows, int row_offset, double* b_dev, void* stream);
+} mgb_generic_device_code;
+/* Register the generic kernels of a module (the last registration wins;
+ * MGB_ERR_ARG on an ABI mismatch), and withdraw them when that module is
+ * unloaded (no effect unless `code` is the one registered). */
+int mgb_register_generic_device_code(const mgb_generic_device_code* code);
+int mgb_unregister_generic_device_code(const mgb_generic_device_code* code);
+
 /* ---------------------------------------------------------- checkpoint I/O */
 /* File format of mpla_save_vector (mpla.cpp:605-652): int32 n, then n float64. */
 int mgb_save_vector(const char* path, int n, const double* x_dev);

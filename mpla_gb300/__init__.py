@@ -48,6 +48,7 @@ C_ABI_SYMBOLS = (
     "mgb_batch_create", "mgb_batch_add", "mgb_batch_run", "mgb_batch_finished", "mgb_batch_result",
     "mgb_batch_tuning", "mgb_batch_destroy",
     "mgb_set_mixed_matvec", "mgb_get_mixed_matvec", "mgb_gauss_mixed_work",
+    "mgb_register_generic_device_code", "mgb_unregister_generic_device_code",
 )
 
 
@@ -107,6 +108,8 @@ _SIGS = {
     "mgb_time_gauss_matvec": (_I, [_I, _I, _P, _D, _I, _P, _P, _I, C.POINTER(_D), _P]),
     "mgb_time_dgemv": (_I, [_I, _P, _P, _P, _I, C.POINTER(_D), _P]),
     "mgb_save_vector": (_I, [C.c_char_p, _I, _P]),
+    "mgb_register_generic_device_code": (_I, [_P]),
+    "mgb_unregister_generic_device_code": (_I, [_P]),
     "mgb_load_vector": (_I, [C.c_char_p, _I, _P]),
     "mgb_batch_create": (_I, [_I, C.POINTER(_P)]),
     "mgb_batch_add": (_I, [_P, _I, _I, _P, _D, _I, _P, _I, _D, _I, C.c_size_t, C.POINTER(_I)]),

@@ -7,8 +7,12 @@
 //   * Gaussian systems — from a kernel_matrix_data descriptor or from an
 //     assembler made by this library's factory — run the fused FP64 kernel
 //     (no matrix storage, so max_row_count_per_dgemv has nothing to bound);
-//   * any other system_assembler runs a fused kernel that calls its virtual
-//     get_matrix_entry per entry, again without storing the matrix.
+//   * any other system_assembler is a user subclass whose device code lives
+//     in the user's module; its virtual get_matrix_entry is called per entry
+//     by a fused kernel of lib/mpla_generic_device.o, which the user
+//     device-links into that module (as MPLA's Makefile:96-114 links
+//     generic_system_adapter.o) and which registers itself here
+//     (mgb_register_generic_device_code); the matrix is never stored.
 #include <cstring>
 #include <mutex>
 #include <set>
@@ -75,45 +79,28 @@ __global__ void k_destroy_gauss(gaussian_kernel_system_assembler** obj) {
   *obj = nullptr;
 }
 
-// Generic fused matvec: one row per thread, a column range per CTA, entries
-// from the object's virtual get_matrix_entry; x staged in shared memory.
-constexpr int kGenThreads = 128;
-constexpr int kGenTileJ = 256;
+// Generic kernels of the user's module (lib/mpla_generic_device.o), set by
+// its static constructor.
+std::mutex g_generic_mutex;
+const mgb_generic_device_code* g_generic_code = nullptr;
 
-__global__ void __launch_bounds__(kGenThreads) k_generic_matvec(system_assembler* assem, int rows, int cols,
-                                                                int row_offset, int col_offset,
-                                                                const double* __restrict__ x, double* __restrict__ y,
-                                                                int cols_per_split, int nsplit,
-                                                                double* __restrict__ partials,
-                                                                unsigned int* __restrict__ tickets,
-                                                                const int* __restrict__ skip) {
-  if (skip && *skip) return;
-  __shared__ double sx[kGenTileJ];
-  __shared__ int s_last;
-  const int tile = blockIdx.x / nsplit, split = blockIdx.x % nsplit;
-  const int i = tile * kGenThreads + threadIdx.x;
-  const int cbeg = split * cols_per_split, cend = min(cols, cbeg + cols_per_split);
-  double acc = 0.0;
-  for (int j0 = cbeg; j0 < cend; j0 += kGenTileJ) {
-    const int nj = min(kGenTileJ, cend - j0);
-    __syncthreads();
-    for (int t = threadIdx.x; t < nj; t += kGenThreads) sx[t] = x[j0 + t];
-    __syncthreads();
-    if (i < rows)
-      for (int t = 0; t < nj; ++t) acc = fma(assem->get_matrix_entry(row_offset + i, col_offset + j0 + t), sx[t], acc);
-  }
-  if (nsplit == 1) {
-    if (i < rows) y[i] = acc;
-    return;
-  }
-  if (i < rows) partials[(long long)split * rows + i] = acc;
-  if (last_block_arrival(&tickets[tile], nsplit, &s_last)) {
-    if (i < rows) {
-      double s = 0.0;
-      for (int p = 0; p < nsplit; ++p) s += __ldcg(&partials[(long long)p * rows + i]);
-      y[i] = s;
-    }
-  }
+const mgb_generic_device_code* generic_code() {
+  std::lock_guard<std::mutex> lock(g_generic_mutex);
+  return g_generic_code;
+}
+
+constexpr int kGenRows = 128;  // rows per CTA of the device-linked kernel
+
+bool is_library_gauss(const void* obj) {
+  std::lock_guard<std::mutex> lock(g_registry_mutex);
+  return obj && g_gauss_objects.count(obj);
+}
+
+int no_generic_code() {
+  return set_error(MGB_ERR_ARG,
+                   "system_assembler object not made by this library's factory, and no device-linked generic "
+                   "adapter is registered: link lib/mpla_generic_device.o with -rdc=true into the module that "
+                   "constructs the assembler");
 }
 
 __global__ void k_generic_rhs(system_assembler* assem, int rows, int row_offset, double* __restrict__ b) {
@@ -141,7 +128,9 @@ class GenericAssemblerMatvec : public Matvec {
   int apply(const double* x, double* y, cudaStream_t s, const int* skip) override {
     const int rows = A_->cur_proc_row_count, cols = A_->cur_proc_col_count;
     if (rows <= 0) return MGB_OK;
-    const int tiles = (rows + kGenThreads - 1) / kGenThreads;
+    const mgb_generic_device_code* code = generic_code();
+    if (!code) return no_generic_code();
+    const int tiles = (rows + kGenRows - 1) / kGenRows;
     int nsplit = (8 * c_->num_sms + tiles - 1) / tiles;
     nsplit = max(1, min(nsplit, (cols + 255) / 256));
     const int cps = (cols + nsplit - 1) / nsplit;
@@ -150,10 +139,10 @@ class GenericAssemblerMatvec : public Matvec {
       MGB_TRY(ensure_split_partials(c_, (size_t)nsplit * rows));
       MGB_TRY(ensure_tickets(c_, tiles + 1));
     }
-    k_generic_matvec<<<tiles * nsplit, kGenThreads, 0, s>>>(static_cast<system_assembler*>(A_->data), rows, cols,
-                                                            A_->cur_proc_row_offset, A_->cur_proc_col_offset, x, y,
-                                                            cps, nsplit, c_->split_partials, c_->tickets + 1, skip); count_launches(1);
-    MGB_CUDA(cudaGetLastError());
+    const int e = code->matvec(A_->data, rows, cols, A_->cur_proc_row_offset, A_->cur_proc_col_offset, x, y, cps,
+                               nsplit, c_->split_partials, c_->tickets + 1, skip, s);
+    if (e != 0) return cuda_error(static_cast<cudaError_t>(e), "device-linked generic matvec", __FILE__, __LINE__);
+    count_launches(1);
     return MGB_OK;
   }
   int n() const override { return A_->cur_proc_row_count; }
@@ -288,10 +277,36 @@ void mpla_set_generic_system_rhs(struct mpla_vector* b, struct mpla_generic_matr
   (void)instance;
   DeviceContext* c = ctx();
   const int rows = A->cur_proc_row_count;
-  k_generic_rhs<<<(rows + 255) / 256, 256, 0, c->stream>>>(static_cast<system_assembler*>(A->data), rows,
-                                                          A->cur_proc_row_offset, b->data); count_launches(1);
+  if (is_library_gauss(A->data)) {
+    // constructed in this module: its virtual get_rhs_entry is callable here
+    k_generic_rhs<<<(rows + 255) / 256, 256, 0, c->stream>>>(static_cast<system_assembler*>(A->data), rows,
+                                                            A->cur_proc_row_offset, b->data);
+    count_launches(1);
+  } else {
+    const mgb_generic_device_code* code = generic_code();
+    if (!code) die(no_generic_code());
+    const int e = code->rhs(A->data, rows, A->cur_proc_row_offset, b->data, c->stream);
+    if (e != 0) die(cuda_error(static_cast<cudaError_t>(e), "device-linked generic rhs", __FILE__, __LINE__));
+    count_launches(1);
+  }
   cudaStreamSynchronize(c->stream);
   checkCUDAError("gen_generic_system_rhs");
+}
+
+extern "C" int mgb_register_generic_device_code(const mgb_generic_device_code* code) {
+  if (code && code->abi_version != MGB_GENERIC_DEVICE_ABI)
+    return set_error(MGB_ERR_ARG, "generic device code ABI %d, library expects %d", code->abi_version,
+                     MGB_GENERIC_DEVICE_ABI);
+  if (code && (!code->matvec || !code->rhs)) return set_error(MGB_ERR_ARG, "generic device code without launchers");
+  std::lock_guard<std::mutex> lock(g_generic_mutex);
+  g_generic_code = code;
+  return MGB_OK;
+}
+
+extern "C" int mgb_unregister_generic_device_code(const mgb_generic_device_code* code) {
+  std::lock_guard<std::mutex> lock(g_generic_mutex);
+  if (g_generic_code == code) g_generic_code = nullptr;
+  return MGB_OK;
 }
 
 // ------------------------------------------ kernel_system_assembler.h factory
