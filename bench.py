@@ -524,6 +524,7 @@ def reference_dense(ref, n: int = 4096, reps: int = 10) -> dict:
 
     A, b, x0 = synth.config_dense(0)
     _, gemv_ms = ref.dgemv(A, np.linspace(-1.0, 1.0, n), reps=50)
+    cublas_ms = ref.cublas_dgemv_ms(A, reps=50)
     for _ in range(2):
         ref.solve_dense(A, b, x0, 1000, EPS, ref.SOLVER_CG_REL)
     times, mvs = [], []
@@ -537,7 +538,9 @@ def reference_dense(ref, n: int = 4096, reps: int = 10) -> dict:
             "solves_per_s": 1e3 / solve_ms, "ms_per_solve": solve_ms,
             "iterations": ref.iterations(ref.SOLVER_CG_REL, mvs[-1]),
             "dgemv": {"ms": gemv_ms, "achieved_gbs": gemv_bytes / (gemv_ms * 1e-3) / 1e9, "bytes": gemv_bytes,
-                      "what": "mpla_dgemv (cuBLAS Dgemv plus the reference's per-call allocations and copies)"}}
+                      "what": "mpla_dgemv (cuBLAS Dgemv plus the reference's per-call allocations and copies)"},
+            "cublas_dgemv": {"ms": cublas_ms, "achieved_gbs": gemv_bytes / (cublas_ms * 1e-3) / 1e9,
+                             "what": "the cublasDgemv call inside mpla_dgemv alone, on resident operands"}}
 
 
 def run_reference(args, world, rank, local):

@@ -168,6 +168,33 @@ int ref_dgemv(int m, int n, const double* A, const double* x, double* y, int rep
   return check();
 }
 
+// The cuBLAS call inside mpla_dgemv (mpla.cpp:729) on its own: cublasDgemv
+// OP_N with the instance's handle on resident A, x, y, `reps` times; mean ms.
+int ref_cublas_dgemv(int n, const double* A, int reps, double* ms) {
+  double *dA = nullptr, *dx = nullptr, *dy = nullptr;
+  cudaMalloc((void**)&dA, sizeof(double) * (size_t)n * n);
+  cudaMalloc((void**)&dx, sizeof(double) * n);
+  cudaMalloc((void**)&dy, sizeof(double) * n);
+  cudaMemcpy(dA, A, sizeof(double) * (size_t)n * n, cudaMemcpyHostToDevice);
+  cudaMemset(dx, 0, sizeof(double) * n);
+  const double one = 1.0, zero = 0.0;
+  cublasDgemv(g_inst.cublas_handle, CUBLAS_OP_N, n, n, &one, dA, n, dx, 1, &zero, dy, 1);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, 0);
+  for (int r = 0; r < reps; ++r) cublasDgemv(g_inst.cublas_handle, CUBLAS_OP_N, n, n, &one, dA, n, dx, 1, &zero, dy, 1);
+  cudaEventRecord(e1, 0);
+  cudaEventSynchronize(e1);
+  float t = 0.f;
+  cudaEventElapsedTime(&t, e0, e1);
+  if (ms) *ms = reps > 0 ? t / reps : 0.0;
+  cudaFree(dA);
+  cudaFree(dx);
+  cudaFree(dy);
+  return check();
+}
+
 int ref_ddot(int n, const double* x, const double* y, double* out) {
   mpla_vector xv, yv;
   vec_from_host(&xv, x, n);

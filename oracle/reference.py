@@ -36,6 +36,7 @@ def lib(device: int = 0):
         L.ref_init.argtypes = [I]
         L.ref_dgemv.argtypes = [I, I, P, P, P, I, C.POINTER(D)]
         L.ref_ddot.argtypes = [I, P, P, C.POINTER(D)]
+        L.ref_cublas_dgemv.argtypes = [I, P, I, C.POINTER(D)]
         L.ref_solve_dense.argtypes = [I, P, P, P, I, D, I, C.POINTER(I), C.POINTER(D)]
         L.ref_gauss_matvec.argtypes = [I, I, P, D, I, P, P]
         L.ref_gauss_rhs.argtypes = [I, I, P, I, P]
@@ -59,6 +60,15 @@ def dgemv(A: np.ndarray, x: np.ndarray, reps: int = 0):
     ms = C.c_double()
     assert lib().ref_dgemv(m, n, A.ctypes.data, x.ctypes.data, y.ctypes.data, reps, C.byref(ms)) == 0
     return y, ms.value
+
+
+def cublas_dgemv_ms(A: np.ndarray, reps: int = 50) -> float:
+    """Mean ms of the reference's own cublasDgemv call (mpla.cpp:729) on a
+    resident square matrix."""
+    A = np.asfortranarray(A, dtype=np.float64)
+    ms = C.c_double()
+    assert lib().ref_cublas_dgemv(A.shape[0], A.ctypes.data, reps, C.byref(ms)) == 0
+    return ms.value
 
 
 def ddot(x, y) -> float:
