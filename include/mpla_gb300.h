@@ -253,6 +253,15 @@ int mgb_unregister_generic_device_code(const mgb_generic_device_code* code);
 int mgb_save_vector(const char* path, int n, const double* x_dev);
 int mgb_load_vector(const char* path, int n, double* x_dev);
 
+/* ------------------------------------------------------ quadrature points */
+/* Halton points (host code, no device needed): point i (0-based) has
+ * coordinate d = the radical inverse of start + i + 1 in the d-th prime base
+ * (2, 3, 5, ...), written structure-of-arrays, points_host[d * n + i],
+ * 1 <= dim <= 16.  The point set of MPLA's quadrature-weight application
+ * (generate_quadrature_weights.cpp:107-173), which takes it from GSL's
+ * gsl_qrng_halton; GSL is not part of this library. */
+int mgb_halton(int n, int dim, long long start, double* points_host);
+
 #ifdef __cplusplus
 }
 #endif

@@ -49,6 +49,7 @@ C_ABI_SYMBOLS = (
     "mgb_batch_tuning", "mgb_batch_destroy",
     "mgb_set_mixed_matvec", "mgb_get_mixed_matvec", "mgb_gauss_mixed_work",
     "mgb_register_generic_device_code", "mgb_unregister_generic_device_code",
+    "mgb_halton",
 )
 
 
@@ -109,6 +110,7 @@ _SIGS = {
     "mgb_time_dgemv": (_I, [_I, _P, _P, _P, _I, C.POINTER(_D), _P]),
     "mgb_save_vector": (_I, [C.c_char_p, _I, _P]),
     "mgb_register_generic_device_code": (_I, [_P]),
+    "mgb_halton": (_I, [_I, _I, C.c_longlong, _P]),
     "mgb_unregister_generic_device_code": (_I, [_P]),
     "mgb_load_vector": (_I, [C.c_char_p, _I, _P]),
     "mgb_batch_create": (_I, [_I, C.POINTER(_P)]),
@@ -274,6 +276,14 @@ def gauss_mixed_work(pts: GaussPoints) -> int:
 
 def get_mixed_matvec() -> int:
     return int(lib().mgb_get_mixed_matvec())
+
+
+def halton(n: int, dim: int, start: int = 0) -> np.ndarray:
+    """Halton points (dim x n) of the quadrature-weight application: host
+    code of the library, no device needed."""
+    out = np.empty((dim, n))
+    check(lib().mgb_halton(n, dim, start, out.ctypes.data))
+    return out
 
 
 def kernel_launches() -> int:

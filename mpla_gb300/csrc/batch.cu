@@ -13,20 +13,31 @@
 //           items of mixed systems: partial K~ d per chunk, entries in FP32
 //           with the exponential on the SFU, summed in FP32 per chunk
 //   mv64    the same items of FP64 systems: partial K d in FP64
-//           (the matvecs of every class and mode run as concurrent branches)
+//   true    one slice of every FP64 true-residual round in progress (below)
+//           (the launches of this phase, per class and kind, run as
+//           concurrent graph branches)
 //   alpha   persistent kernel over (system, 1024-row) items: z = nugget d +
 //           the chunk partials in chunk order, per-item <d,z>; the last item
 //           of a system to finish sums the items in order and sets alpha
 //   update  x += alpha d, r -= alpha z, <r,r>; the last item sets beta, the
 //           stop test, and for mixed lanes whether the FP64 true residual is
-//           due
-//   mv64r   (system, 128 rows) items of mixed systems with a pending
-//           replacement: z = b - K x for the lanes that are due, FP64
-//           entries, products and sums in double-double
-//   replace r = z for those lanes, convergence test on the FP64 true
-//           residual, restart of the direction
+//           due (such a lane then waits for a true-residual round)
+//   replace r = b - K x for the lanes of a completed round, convergence test
+//           on the FP64 true residual, restart of the direction
 //   dir     d = beta d + r (and its FP32 copy)
-//   count   lanes still running per system, systems still running
+//   count   lanes still running per system, systems still running; starts
+//           and advances the true-residual rounds
+// True residuals run in the background of the other systems' iterations.
+// A round serves the lanes of one system that were waiting when it started
+// (they stop iterating until it ends; the system's other lanes go on).  It
+// splits the columns into streams of kTrueSpan 128-column tiles; in each
+// step every (row tile, stream) item adds the next column tile of its stream
+// to its double-double sums, so the round takes min(tiles, kTrueSpan) steps,
+// each step's FP64 work is one tile pair per item (it overlaps the FP32
+// matvecs, which use other pipes), and the sums are added in an order fixed
+// by the system alone.  (Computing a whole residual inside one step, as
+// before, stalled every system for the ~30 ms a n = 15000 residual takes on
+// GB300's FP64 pipe, and most steps of a 512-system batch held one.)
 // Work is split so that one large system still spreads over the whole GPU,
 // and every sum runs in an order fixed by the system's own size: a system's
 // result is bitwise the same alone and in any mix.  Systems and item lists
@@ -64,9 +75,10 @@ constexpr int kColTile = 128;     // columns staged per shared-memory round
 constexpr int kChunkCols = 1024;  // columns per matvec item
 constexpr int kVecThreads = 256;  // threads of the vector-phase CTAs
 constexpr int kVecRows = 1024;    // rows per vector-phase item
+constexpr int kTrueSpan = 32;     // column tiles per stream of a true-residual round
 
 enum LaneDone : int { LANE_RUNNING = 0, LANE_CONVERGED = 1, LANE_CAPPED = 2, LANE_BROKE = 3 };
-enum QueueMode : int { Q_MV32 = 0, Q_MV64 = 1, Q_MV64_TRUE = 2 };
+enum QueueMode : int { Q_MV32 = 0, Q_MV64 = 1 };
 
 __device__ __forceinline__ float ex2_approx(float v) {
   float r;
@@ -75,6 +87,8 @@ __device__ __forceinline__ float ex2_approx(float v) {
 }
 
 __device__ __forceinline__ bool sys_active(const BatchSys& s) { return s.in_use && s.active_lanes > 0; }
+// a lane that iterates this step: running and not waiting for a true residual
+__device__ __forceinline__ bool lane_live(const BatchLane& L) { return L.done == LANE_RUNNING && L.hi == 0; }
 
 // Persistent work loop shared by the matvec kernels: items are claimed with
 // an atomic counter that the last CTA to finish resets for the next launch.
@@ -156,7 +170,7 @@ __global__ void __launch_bounds__(kTile) k_bmv32(WorkQueue q, const BatchSys* __
     if (it >= *q.count) break;
     const BatchItem w = q.items[it];
     const BatchSys& S = sys[w.sys];
-    if (!sys_active(S) || S.precision != MGB_PREC_MIXED || S.dim != DIM || S.R != R) continue;
+    if (!sys_active(S) || S.live_lanes == 0 || S.precision != MGB_PREC_MIXED || S.dim != DIM || S.R != R) continue;
     // items are 128-row tiles; a variant with RPT rows per thread covers
     // RPT consecutive tiles and takes only every RPT-th item
     if ((w.row0 / kTile) % RPT != 0) continue;
@@ -251,26 +265,9 @@ __global__ void __launch_bounds__(kTile) k_bmv32(WorkQueue q, const BatchSys* __
 }
 
 // ------------------------------------------------------- FP64 matvec
-// TRUE_RES = false: partial K d over one column chunk of FP64 systems, into
-// P[chunk] (the reference's FP64 iteration).  TRUE_RES = true: the true
-// residual z = b - (K x + nugget x) of mixed systems with a pending
-// replacement, whole rows (the chunk-0 items only).  On these systems x
-// reaches ~1e4 ||b||, and a plain FP64 sum of K_ij x_j over a row carries
-// noise of about u * sum_j |K_ij x_j|, i.e. ~1e-10 relative: the very
-// tolerance the mixed iteration must certify (points are in the caller's
-// order, so even a 128-column tile mixes far-apart large terms).  So every
-// product is split exactly by an FMA and summed in double-double (TwoSum,
-// Knuth, TAOCP vol. 2, 4.2.2): the compensated dot product of Ogita, Rump
-// and Oishi.
-__device__ __forceinline__ void dd_add(double& s, double& c, double p, double pe) {
-  const double t = __dadd_rn(s, p);
-  const double bp = __dsub_rn(t, s);
-  const double e = __dadd_rn(__dsub_rn(s, __dsub_rn(t, bp)), __dsub_rn(p, bp));
-  s = t;
-  c = __dadd_rn(c, __dadd_rn(e, pe));
-}
-
-template <int DIM, int R, bool TRUE_RES>
+// Partial K d over one column chunk of FP64 systems, into P[chunk] (the
+// reference's FP64 iteration).
+template <int DIM, int R>
 __global__ void __launch_bounds__(kTile) k_bmv64(WorkQueue q, const BatchSys* __restrict__ sys,
                                                  const double* __restrict__ table_g) {
   __shared__ double table[kExpTableSize];
@@ -283,30 +280,20 @@ __global__ void __launch_bounds__(kTile) k_bmv64(WorkQueue q, const BatchSys* __
     if (it >= *q.count) break;
     const BatchItem w = q.items[it];
     const BatchSys& S = sys[w.sys];
-    if (!sys_active(S) || S.dim != DIM || S.R != R) continue;
-    if (!TRUE_RES && S.precision != MGB_PREC_FP64) continue;
-    if (TRUE_RES && (S.precision != MGB_PREC_MIXED || !S.need_hi || w.chunk != 0)) continue;
+    if (!sys_active(S) || S.dim != DIM || S.R != R || S.precision != MGB_PREC_FP64) continue;
     if (!have_table) {
       for (int i = threadIdx.x; i < kExpTableSize; i += kTile) table[i] = table_g[i];
       have_table = true;  // the __syncthreads of the column staging below orders it
     }
     const int n = S.n;
-    const double* v = TRUE_RES ? S.x : S.d;
     const int i = w.row0 + threadIdx.x;
-    // true residuals only for the lanes whose replacement is due (the
-    // others, and padding lanes, would cost 8 FP64 operations per entry for
-    // a z that nothing reads); the same for every thread, so no divergence
-    bool on[R];
-#pragma unroll
-    for (int k = 0; k < R; ++k) on[k] = !TRUE_RES || (S.lanes[k].done == LANE_RUNNING && S.lanes[k].flag);
-    const int c0 = TRUE_RES ? 0 : w.chunk * kChunkCols;
-    const int c1 = TRUE_RES ? n : min(n, c0 + kChunkCols);
+    const int c0 = w.chunk * kChunkCols, c1 = min(n, c0 + kChunkCols);
     double pi[DIM];
 #pragma unroll
     for (int d = 0; d < DIM; ++d) pi[d] = S.pts64[(long long)d * n + min(i, n - 1)];
-    double acc[R], cmp[R];
+    double acc[R];
 #pragma unroll
-    for (int k = 0; k < R; ++k) acc[k] = cmp[k] = 0.0;
+    for (int k = 0; k < R; ++k) acc[k] = 0.0;
     for (int j0 = c0; j0 < c1; j0 += kColTile) {
       const int nj = min(kColTile, c1 - j0);
       __syncthreads();
@@ -315,7 +302,7 @@ __global__ void __launch_bounds__(kTile) k_bmv64(WorkQueue q, const BatchSys* __
 #pragma unroll
         for (int d = 0; d < DIM; ++d) sp[d][t] = in ? S.pts64[(long long)d * n + j0 + t] : 0.0;
 #pragma unroll
-        for (int k = 0; k < R; ++k) sv[t * R + k] = in ? v[(long long)(j0 + t) * R + k] : 0.0;
+        for (int k = 0; k < R; ++k) sv[t * R + k] = in ? S.d[(long long)(j0 + t) * R + k] : 0.0;
       }
       __syncthreads();
       double tile[R];
@@ -330,39 +317,119 @@ __global__ void __launch_bounds__(kTile) k_bmv64(WorkQueue q, const BatchSys* __
         }
         const double e = exp_neg_table(s, table);
 #pragma unroll
-        for (int k = 0; k < R; ++k) {
-          const double vk = sv[t * R + k];
-          if (TRUE_RES) {
-            if (on[k]) {
-              const double p = __dmul_rn(e, vk);
-              dd_add(acc[k], cmp[k], p, fma(e, vk, -p));
-            }
-          } else {
-            tile[k] = fma(e, vk, tile[k]);
-          }
-        }
+        for (int k = 0; k < R; ++k) tile[k] = fma(e, sv[t * R + k], tile[k]);
       }
-      if (!TRUE_RES)
 #pragma unroll
-        for (int k = 0; k < R; ++k) acc[k] += tile[k];
+      for (int k = 0; k < R; ++k) acc[k] += tile[k];
     }
     if (i < n) {
 #pragma unroll
-      for (int k = 0; k < R; ++k) {
-        const long long o = (long long)i * R + k;
-        if (TRUE_RES) {
-          if (!on[k]) continue;
-          const double p = __dmul_rn(S.nugget, v[o]);
-          dd_add(acc[k], cmp[k], p, fma(S.nugget, v[o], -p));
-          // b and acc agree to a few digits, so b - acc is (nearly) exact
-          S.z[o] = __dsub_rn(__dsub_rn(S.b[o], acc[k]), cmp[k]);
-        } else {
-          S.P[((long long)w.chunk * n + i) * R + k] = acc[k];
+      for (int k = 0; k < R; ++k) S.P[((long long)w.chunk * n + i) * R + k] = acc[k];
+    }
+  }
+  queue_done(q);
+}
+
+// ---------------------------------------------------- FP64 true residuals
+// The true residual z = b - (K x + nugget x) of the mixed lanes in a round.
+// On these systems x reaches ~1e4 ||b||, and a plain FP64 sum of K_ij x_j
+// over a row carries noise of about u * sum_j |K_ij x_j|, i.e. ~1e-10
+// relative: the very tolerance the mixed iteration must certify (points are
+// in the caller's order, so even a 128-column tile mixes far-apart large
+// terms).  So every product is split exactly by an FMA and summed in
+// double-double (TwoSum, Knuth, TAOCP vol. 2, 4.2.2): the compensated dot
+// product of Ogita, Rump and Oishi.
+__device__ __forceinline__ void dd_add(double& s, double& c, double p, double pe) {
+  const double t = __dadd_rn(s, p);
+  const double bp = __dsub_rn(t, s);
+  const double e = __dadd_rn(__dsub_rn(s, __dsub_rn(t, bp)), __dsub_rn(p, bp));
+  s = t;
+  c = __dadd_rn(c, __dadd_rn(e, pe));
+}
+
+// One step of every round in progress: item (row tile I, stream c) of a
+// system adds column tile J = c * kTrueSpan + hi_step of its stream to the
+// double-double sums of its 128 rows (zt[c], zero at the round's first
+// step).  The systems come from the list the count phase builds; the items
+// of all of them are dealt round-robin to the CTAs of the launch.
+template <int DIM, int R>
+__global__ void __launch_bounds__(kTile) k_btrue(const int* __restrict__ pending, const int* __restrict__ npending,
+                                                 BatchSys* __restrict__ sys, const double* __restrict__ table_g) {
+  __shared__ double table[kExpTableSize];
+  __shared__ double sp[DIM][kTile];
+  __shared__ double sv[kTile * R];
+  bool have_table = false;
+  const int np = *npending;
+  long long base = 0;  // index of the current system's first item
+  for (int p = 0; p < np; ++p) {
+    BatchSys& S = sys[pending[p]];
+    if (S.dim != DIM || S.R != R) continue;
+    const int n = S.n, T = (n + kTile - 1) / kTile, step = S.hi_step;
+    const long long nitems = (long long)T * S.nstream;
+    long long k = ((long long)blockIdx.x - base) % gridDim.x;
+    if (k < 0) k += gridDim.x;
+    base += nitems;
+    bool on[R];
+#pragma unroll
+    for (int l = 0; l < R; ++l) on[l] = S.lanes[l].done == LANE_RUNNING && S.lanes[l].hi == 2;
+    for (; k < nitems; k += gridDim.x) {
+      const int I = (int)(k % T), c = (int)(k / T);
+      const int J = c * kTrueSpan + step;
+      if (J >= T) continue;
+      if (!have_table) {
+        for (int t = threadIdx.x; t < kExpTableSize; t += kTile) table[t] = table_g[t];
+        have_table = true;  // ordered by the __syncthreads below
+      }
+      const int i = I * kTile + threadIdx.x;
+      const int j0 = J * kTile, nj = min(kTile, n - j0);
+      double* zs = S.zt + (size_t)c * n * R * 2;
+      double acc[R], cmp[R];
+#pragma unroll
+      for (int l = 0; l < R; ++l) {
+        acc[l] = cmp[l] = 0.0;
+        if (step > 0 && i < n && on[l]) {
+          acc[l] = zs[((size_t)i * R + l) * 2];
+          cmp[l] = zs[((size_t)i * R + l) * 2 + 1];
+        }
+      }
+      __syncthreads();  // the previous item is done with sp / sv
+      for (int t = threadIdx.x; t < kTile; t += kTile) {
+        const bool in = t < nj;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) sp[d][t] = in ? S.pts64[(long long)d * n + j0 + t] : 0.0;
+#pragma unroll
+        for (int l = 0; l < R; ++l) sv[t * R + l] = in ? S.x[(long long)(j0 + t) * R + l] : 0.0;
+      }
+      __syncthreads();
+      double pi[DIM];
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) pi[d] = S.pts64[(long long)d * n + min(i, n - 1)];
+      for (int t = 0; t < nj; ++t) {
+        double s2 = 0.0;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          const double df = pi[d] - sp[d][t];
+          s2 = (d == 0) ? df * df : fma(df, df, s2);
+        }
+        const double e = exp_neg_table(s2, table);
+#pragma unroll
+        for (int l = 0; l < R; ++l) {
+          if (!on[l]) continue;
+          const double vl = sv[t * R + l];
+          const double pr = __dmul_rn(e, vl);
+          dd_add(acc[l], cmp[l], pr, fma(e, vl, -pr));
+        }
+      }
+      if (i < n) {
+#pragma unroll
+        for (int l = 0; l < R; ++l) {
+          if (!on[l]) continue;
+          zs[((size_t)i * R + l) * 2] = acc[l];
+          zs[((size_t)i * R + l) * 2 + 1] = cmp[l];
         }
       }
     }
   }
-  queue_done(q);
 }
 
 // ---------------------------------------------------------- vector phases
@@ -430,7 +497,7 @@ __device__ void vec_alpha(BatchSys& S, int row0, double* smem, int* s_last) {
   if (!finish_item<R>(S, row0 / kVecRows, v, smem, s_last, tot)) return;
   if (threadIdx.x < R) {
     BatchLane& L = S.lanes[threadIdx.x];
-    if (L.done == LANE_RUNNING) {
+    if (lane_live(L)) {
       const double a = L.rr / tot[threadIdx.x];
       if (!(tot[threadIdx.x] > 0.0) || !isfinite(a)) L.done = LANE_BROKE;
       else L.alpha = a;
@@ -444,7 +511,7 @@ __device__ void vec_update(BatchSys& S, int row0, double* smem, int* s_last, dou
   __shared__ int s_run[8];
   if (threadIdx.x < R) {
     s_alpha[threadIdx.x] = S.lanes[threadIdx.x].alpha;
-    s_run[threadIdx.x] = S.lanes[threadIdx.x].done == LANE_RUNNING;
+    s_run[threadIdx.x] = lane_live(S.lanes[threadIdx.x]);
   }
   __syncthreads();
   double v[R];
@@ -466,19 +533,17 @@ __device__ void vec_update(BatchSys& S, int row0, double* smem, int* s_last, dou
   double tot[8];
   if (!finish_item<R>(S, row0 / kVecRows, v, smem, s_last, tot)) return;
   if (threadIdx.x == 0) {
-    int need = 0;
     for (int k = 0; k < R; ++k) {
       BatchLane& L = S.lanes[k];
-      if (L.done != LANE_RUNNING) continue;
+      if (!s_run[k]) continue;
       L.k += 1;
       const double rr_new = tot[k];
       if (S.precision == MGB_PREC_MIXED) {
         const bool replace = (rr_new < delta2 * L.rr_ref) || (sqrt(rr_new) / L.bnorm < S.eps) ||
                              (L.k + 1 >= S.iter_max) || !(rr_new == rr_new);
         L.rr_new = rr_new;
-        L.flag = replace ? 1 : 0;
         if (replace) {
-          need = 1;
+          L.hi = 1;  // waits (does not iterate) until a true-residual round has served it
         } else {
           L.beta = rr_new / L.rr;
           L.rr = rr_new;
@@ -492,25 +557,36 @@ __device__ void vec_update(BatchSys& S, int row0, double* smem, int* s_last, dou
         else if (L.k + 1 >= S.iter_max) L.done = LANE_CAPPED;
       }
     }
-    S.need_hi = need;
   }
 }
 
+// Lanes of a completed true-residual round: r = b - (sum of the streams in
+// order + nugget x), all in double-double, then the convergence test and a
+// restart of the direction from the true residual.
 template <int R>
 __device__ void vec_replace(BatchSys& S, int row0, double* smem, int* s_last) {
   __shared__ int s_flag[8];
-  if (threadIdx.x < R) s_flag[threadIdx.x] = S.lanes[threadIdx.x].done == LANE_RUNNING && S.lanes[threadIdx.x].flag;
+  if (threadIdx.x < R) s_flag[threadIdx.x] = S.lanes[threadIdx.x].done == LANE_RUNNING && S.lanes[threadIdx.x].hi == 2;
   __syncthreads();
   double v[R];
 #pragma unroll
   for (int k = 0; k < R; ++k) v[k] = 0.0;
-  const int row1 = min(S.n, row0 + kVecRows);
+  const int n = S.n, row1 = min(n, row0 + kVecRows);
   for (int i = row0 + threadIdx.x; i < row1; i += kVecThreads) {
 #pragma unroll
     for (int k = 0; k < R; ++k) {
       if (!s_flag[k]) continue;
       const long long o = (long long)i * R + k;
-      const double ri = S.z[o];  // b - K x from the true-residual matvec
+      double acc = 0.0, cmp = 0.0;
+      for (int c = 0; c < S.nstream; ++c) {
+        const double* zs = S.zt + ((size_t)c * n * R + o) * 2;
+        dd_add(acc, cmp, zs[0], zs[1]);
+      }
+      const double xv = S.x[o];
+      const double p = __dmul_rn(S.nugget, xv);
+      dd_add(acc, cmp, p, fma(S.nugget, xv, -p));
+      // b and acc agree to a few digits, so b - acc is (nearly) exact
+      const double ri = __dsub_rn(__dsub_rn(S.b[o], acc), cmp);
       S.r[o] = ri;
       v[k] = fma(ri, ri, v[k]);
     }
@@ -526,12 +602,12 @@ __device__ void vec_replace(BatchSys& S, int row0, double* smem, int* s_last) {
       L.beta = 0.0;  // restart the direction from the true residual
       L.rr = tot[k];
       L.rr_ref = tot[k];
-      L.flag = 0;
+      L.hi = 0;
       if (L.res < S.eps) L.done = LANE_CONVERGED;
       else if (!(L.res == L.res)) L.done = LANE_BROKE;
       else if (L.k + 1 >= S.iter_max) L.done = LANE_CAPPED;
     }
-    S.need_hi = 0;
+    S.hi_ready = 0;
   }
 }
 
@@ -541,7 +617,7 @@ __device__ void vec_direction(BatchSys& S, int row0) {
   __shared__ int s_run[8];
   if (threadIdx.x < R) {
     s_beta[threadIdx.x] = S.lanes[threadIdx.x].beta;
-    s_run[threadIdx.x] = S.lanes[threadIdx.x].done == LANE_RUNNING;
+    s_run[threadIdx.x] = lane_live(S.lanes[threadIdx.x]);
   }
   __syncthreads();
   const int row1 = min(S.n, row0 + kVecRows);
@@ -557,9 +633,9 @@ __device__ void vec_direction(BatchSys& S, int row0) {
 }
 
 // One persistent kernel per phase; the R dispatch is a runtime switch over
-// templated bodies.  Phase 2 (replace) touches only systems with a pending
-// true residual; every item of such a system takes part, so the last-arrival
-// count is complete.
+// templated bodies.  Phase 2 (replace) touches only systems with a completed
+// true-residual round; every item of such a system takes part, so the
+// last-arrival count is complete.
 template <int PHASE>
 __global__ void __launch_bounds__(kVecThreads) k_bvec(WorkQueue q, const VecItem* __restrict__ vitems,
                                                       BatchSys* sys, double delta2) {
@@ -571,7 +647,7 @@ __global__ void __launch_bounds__(kVecThreads) k_bvec(WorkQueue q, const VecItem
     const VecItem w = vitems[it];
     BatchSys& S = sys[w.sys];
     if (!sys_active(S)) continue;
-    if (PHASE == 2 && (S.precision != MGB_PREC_MIXED || !S.need_hi)) continue;
+    if (PHASE == 2 && (S.precision != MGB_PREC_MIXED || !S.hi_ready)) continue;
     switch (S.R) {
 #define MGB_BVEC_CASE(RR)                                             \
   case RR:                                                            \
@@ -626,31 +702,85 @@ __global__ void __launch_bounds__(kVecThreads) k_binit(BatchSys* sys, int slot) 
       act += L.done == LANE_RUNNING;
     }
     S.active_lanes = act;
-    S.need_hi = 0;
+    S.live_lanes = act;
+    S.hi_step = -1;
+    S.hi_ready = 0;
     *S.ticket = 0u;
   }
 }
 
-// End of a step: lanes still running per system, systems still running.
-__global__ void k_bcount(BatchSys* sys, int nslots, int* active) {
-  __shared__ int sm[32];
+// End of a step: advances the true-residual rounds (the one in progress took
+// its step in this step's matvec phase; a finished one is replaced in the
+// next step; a new one starts for the lanes that wait), counts the lanes
+// still running and iterating per system and the systems still running, and
+// lists the systems with a round in progress in slot order (for the next
+// step's true-residual launches).  One CTA of 256 threads.
+__global__ void __launch_bounds__(256) k_bcount(BatchSys* sys, int nslots, int* active, int* pending,
+                                                int* npending) {
+  __shared__ int sm[8];
+  __shared__ int s_base;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int a = 0;
   for (int s = threadIdx.x; s < nslots; s += blockDim.x) {
     BatchSys& S = sys[s];
     if (!S.in_use) continue;
-    int act = 0;
-    for (int k = 0; k < S.R; ++k) act += S.lanes[k].done == LANE_RUNNING;
+    if (S.precision == MGB_PREC_MIXED) {
+      if (S.hi_step >= 0) {
+        const int T = (S.n + kTile - 1) / kTile;
+        S.hi_step += 1;
+        if (S.hi_step >= min(T, kTrueSpan)) {
+          S.hi_step = -1;
+          S.hi_ready = 1;
+        }
+      }
+      if (S.hi_step < 0 && !S.hi_ready) {
+        int due = 0;
+        for (int k = 0; k < S.R; ++k)
+          if (S.lanes[k].done == LANE_RUNNING && S.lanes[k].hi == 1) {
+            S.lanes[k].hi = 2;
+            ++due;
+          }
+        if (due) S.hi_step = 0;
+      }
+    }
+    int act = 0, live = 0;
+    for (int k = 0; k < S.R; ++k) {
+      act += S.lanes[k].done == LANE_RUNNING;
+      live += lane_live(S.lanes[k]);
+    }
     S.active_lanes = act;
+    S.live_lanes = live;
     a += act > 0 ? 1 : 0;
   }
   a = __reduce_add_sync(0xffffffffu, a);
-  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = a;
+  if (lane == 0) sm[warp] = a;
+  if (threadIdx.x == 0) s_base = 0;
   __syncthreads();
   if (threadIdx.x == 0) {
     int t = 0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sm[w];
     *active = t;
   }
+  __syncthreads();
+  // compaction in slot order (each thread re-reads the slots it updated)
+  for (int s0 = 0; s0 < nslots; s0 += blockDim.x) {
+    const int s = s0 + threadIdx.x;
+    const bool pend = s < nslots && sys[s].in_use && sys[s].precision == MGB_PREC_MIXED && sys[s].hi_step >= 0;
+    const unsigned int m = __ballot_sync(0xffffffffu, pend);
+    if (lane == 0) sm[warp] = __popc(m);
+    __syncthreads();
+    int off = s_base;
+    for (int w = 0; w < warp; ++w) off += sm[w];
+    if (pend) pending[off + __popc(m & ((1u << lane) - 1u))] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int t = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sm[w];
+      s_base += t;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *npending = s_base;
 }
 
 int padded_rhs(int r) { return r <= 1 ? 1 : (r <= 2 ? 2 : (r <= 4 ? 4 : 8)); }
@@ -674,6 +804,7 @@ int BatchEngine::init(DeviceContext* c, int max_systems, cudaStream_t s) {
       MGB_TRY(pool_alloc(c, sizeof(BatchItem) * list_capacity(l), (void**)&items_[l][q]));
   for (int q = 0; q < kClasses; ++q) items_host_[q].clear();
   MGB_TRY(pool_alloc(c, sizeof(VecItem) * max_items_, (void**)&vitems_));
+  MGB_TRY(pool_alloc(c, sizeof(int) * max_systems, (void**)&pending_));
   vitems_host_.clear();
   MGB_TRY(pool_alloc(c, sizeof(int) * kCounterInts, (void**)&counters_));
   MGB_CUDA(cudaMemsetAsync(counters_, 0, sizeof(int) * kCounterInts, s));
@@ -697,6 +828,7 @@ BatchEngine::~BatchEngine() {
     for (int q = 0; q < kClasses; ++q)
       if (items_[l][q]) pool_free(c_, items_[l][q]);
   if (vitems_) pool_free(c_, vitems_);
+  if (pending_) pool_free(c_, pending_);
   if (counters_) pool_free(c_, counters_);
   if (dev_sys_) pool_free(c_, dev_sys_);
   if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
@@ -715,6 +847,7 @@ int BatchEngine::class_of(int dim, int R) {
 }
 
 static int chunks_of(int n) { return (n + kChunkCols - 1) / kChunkCols; }
+static int streams_of(int n) { return ((n + kTile - 1) / kTile + kTrueSpan - 1) / kTrueSpan; }
 static int vec_items_of(int n) { return (n + kVecRows - 1) / kVecRows; }
 
 size_t BatchEngine::bytes_needed(int n, int dim, int nrhs, int precision) {
@@ -725,7 +858,8 @@ size_t BatchEngine::bytes_needed(int n, int dim, int nrhs, int precision) {
   b += sizeof(double) * nv * chunks_of(n) + pad;        // matvec partials
   b += sizeof(double) * 8 * vec_items_of(n) + pad;      // vector-phase partials
   b += sizeof(unsigned int) + pad;                      // ticket
-  if (precision == MGB_PREC_MIXED) b += (sizeof(float4) * (size_t)n + pad) + sizeof(float) * nv + pad;
+  if (precision == MGB_PREC_MIXED)
+    b += (sizeof(float4) * (size_t)n + pad) + sizeof(float) * nv + pad + sizeof(double) * 2 * nv * streams_of(n) + pad;
   return b;
 }
 
@@ -747,15 +881,13 @@ int BatchEngine::add(int n, int dim, const double* coords_host, double nugget, i
   const int nchunks = chunks_of(n), nvec = vec_items_of(n);
   {
     const long long tiles = (n + kTile - 1) / kTile;
-    const long long add_items[kLists] = {tiles * nchunks, (tiles + 1) / 2 * nchunks, (tiles + 3) / 4 * nchunks,
-                                         tiles};
+    const long long add_items[kLists] = {tiles * nchunks, (tiles + 1) / 2 * nchunks, (tiles + 3) / 4 * nchunks};
     long long have[kLists] = {};
     for (const BatchItem& w : items_host_[cls]) {
       const int t = w.row0 / kTile;
       have[kListAll] += 1;
       have[kListRpt2] += t % 2 == 0;
       have[kListRpt4] += t % 4 == 0;
-      have[kListTrue] += w.chunk == 0;
     }
     bool fits = (long long)vitems_host_.size() + nvec <= max_items_;
     for (int l = 0; l < kLists; ++l) fits = fits && have[l] + add_items[l] <= list_capacity(l);
@@ -780,6 +912,8 @@ int BatchEngine::add(int n, int dim, const double* coords_host, double nugget, i
   S.nugget = nugget;
   S.nchunks = nchunks;
   S.nvec = nvec;
+  S.nstream = streams_of(n);
+  S.hi_step = -1;
   char* base = nullptr;
   MGB_TRY(pool_alloc(c_, need, (void**)&base));
   blocks_[slot] = base;
@@ -802,6 +936,7 @@ int BatchEngine::add(int n, int dim, const double* coords_host, double nugget, i
   if (precision == MGB_PREC_MIXED) {
     S.pts_hi = (const float4*)take(sizeof(float4) * (size_t)n);
     S.d32 = (float*)take(sizeof(float) * nv);
+    S.zt = (double*)take(sizeof(double) * 2 * nv * S.nstream);
   }
   // host staging: interleave b; scaled coordinates rounded once to FP32
   std::vector<double> bh(nv, 0.0);
@@ -892,7 +1027,6 @@ int BatchEngine::sync_items() {
       list_host_[kListAll][q].push_back(w);
       if (t % 2 == 0) list_host_[kListRpt2][q].push_back(w);
       if (t % 4 == 0) list_host_[kListRpt4][q].push_back(w);
-      if (w.chunk == 0) list_host_[kListTrue][q].push_back(w);
     }
     for (int l = 0; l < kLists; ++l) {
       const int cnt = (int)list_host_[l][q].size();
@@ -958,27 +1092,44 @@ int BatchEngine::enqueue_mv32(int cls, int rpt, cudaStream_t s) {
 }
 
 template <int DIM, int R>
-static void launch_mv64(const WorkQueue& q, const BatchSys* sys, bool true_res, const double* table, int grid,
-                        cudaStream_t s) {
-  if (true_res) k_bmv64<DIM, R, true><<<grid, kTile, 0, s>>>(q, sys, table);
-  else k_bmv64<DIM, R, false><<<grid, kTile, 0, s>>>(q, sys, table);
+static void launch_mv64(const WorkQueue& q, const BatchSys* sys, const double* table, int grid, cudaStream_t s) {
+  k_bmv64<DIM, R><<<grid, kTile, 0, s>>>(q, sys, table);
 }
 
 int BatchEngine::enqueue_mv64(int cls, int mode, cudaStream_t s) {
-  const int list = mode == Q_MV64_TRUE ? kListTrue : kListAll;
-  const WorkQueue q = make_queue(items_[list][cls], counters_, cls, mode, list);
+  const WorkQueue q = make_queue(items_[kListAll][cls], counters_, cls, mode, kListAll);
   const int grid = 2 * c_->num_sms;
   const double* t = c_->exp_table;
-  const bool tr = mode == Q_MV64_TRUE;
   switch (cls) {
-    case 0: launch_mv64<2, 1>(q, dev_sys_, tr, t, grid, s); break;
-    case 1: launch_mv64<2, 2>(q, dev_sys_, tr, t, grid, s); break;
-    case 2: launch_mv64<2, 4>(q, dev_sys_, tr, t, grid, s); break;
-    case 3: launch_mv64<2, 8>(q, dev_sys_, tr, t, grid, s); break;
-    case 4: launch_mv64<3, 1>(q, dev_sys_, tr, t, grid, s); break;
-    case 5: launch_mv64<3, 2>(q, dev_sys_, tr, t, grid, s); break;
-    case 6: launch_mv64<3, 4>(q, dev_sys_, tr, t, grid, s); break;
-    default: launch_mv64<3, 8>(q, dev_sys_, tr, t, grid, s); break;
+    case 0: launch_mv64<2, 1>(q, dev_sys_, t, grid, s); break;
+    case 1: launch_mv64<2, 2>(q, dev_sys_, t, grid, s); break;
+    case 2: launch_mv64<2, 4>(q, dev_sys_, t, grid, s); break;
+    case 3: launch_mv64<2, 8>(q, dev_sys_, t, grid, s); break;
+    case 4: launch_mv64<3, 1>(q, dev_sys_, t, grid, s); break;
+    case 5: launch_mv64<3, 2>(q, dev_sys_, t, grid, s); break;
+    case 6: launch_mv64<3, 4>(q, dev_sys_, t, grid, s); break;
+    default: launch_mv64<3, 8>(q, dev_sys_, t, grid, s); break;
+  }
+  count_launches(1);
+  MGB_CUDA(cudaGetLastError());
+  return MGB_OK;
+}
+
+// One step of the true-residual rounds of class `cls` (systems listed by the
+// previous step's count phase).
+int BatchEngine::enqueue_true(int cls, cudaStream_t s) {
+  const int grid = 2 * c_->num_sms;
+  const int* np = counters_ + kOffPending;
+  const double* t = c_->exp_table;
+  switch (cls) {
+    case 0: k_btrue<2, 1><<<grid, kTile, 0, s>>>(pending_, np, dev_sys_, t); break;
+    case 1: k_btrue<2, 2><<<grid, kTile, 0, s>>>(pending_, np, dev_sys_, t); break;
+    case 2: k_btrue<2, 4><<<grid, kTile, 0, s>>>(pending_, np, dev_sys_, t); break;
+    case 3: k_btrue<2, 8><<<grid, kTile, 0, s>>>(pending_, np, dev_sys_, t); break;
+    case 4: k_btrue<3, 1><<<grid, kTile, 0, s>>>(pending_, np, dev_sys_, t); break;
+    case 5: k_btrue<3, 2><<<grid, kTile, 0, s>>>(pending_, np, dev_sys_, t); break;
+    case 6: k_btrue<3, 4><<<grid, kTile, 0, s>>>(pending_, np, dev_sys_, t); break;
+    default: k_btrue<3, 8><<<grid, kTile, 0, s>>>(pending_, np, dev_sys_, t); break;
   }
   count_launches(1);
   MGB_CUDA(cudaGetLastError());
@@ -1025,26 +1176,22 @@ int BatchEngine::join_branches(int nb) {
 
 int BatchEngine::enqueue_step() {
   int nb = 0;
-  for (int cls = 0; cls < kClasses; ++cls) nb += (int)has_mixed_[cls] + (int)has_fp64_[cls];
+  for (int cls = 0; cls < kClasses; ++cls) nb += 2 * (int)has_mixed_[cls] + (int)has_fp64_[cls];
   MGB_TRY(fork_branches(nb));
   nb = 0;
   for (int cls = 0; cls < kClasses; ++cls) {
-    if (has_mixed_[cls]) MGB_TRY(enqueue_mv32(cls, rpt_[cls] ? rpt_[cls] : 2, side_[nb++]));
+    if (has_mixed_[cls]) {
+      MGB_TRY(enqueue_mv32(cls, rpt_[cls] ? rpt_[cls] : 2, side_[nb++]));
+      MGB_TRY(enqueue_true(cls, side_[nb++]));
+    }
     if (has_fp64_[cls]) MGB_TRY(enqueue_mv64(cls, Q_MV64, side_[nb++]));
   }
   MGB_TRY(join_branches(nb));
   MGB_TRY(enqueue_vec(0));
   MGB_TRY(enqueue_vec(1));
-  nb = 0;
-  for (int cls = 0; cls < kClasses; ++cls) nb += (int)has_mixed_[cls];
-  MGB_TRY(fork_branches(nb));
-  nb = 0;
-  for (int cls = 0; cls < kClasses; ++cls)
-    if (has_mixed_[cls]) MGB_TRY(enqueue_mv64(cls, Q_MV64_TRUE, side_[nb++]));
-  MGB_TRY(join_branches(nb));
   MGB_TRY(enqueue_vec(2));
   MGB_TRY(enqueue_vec(3));
-  k_bcount<<<1, 256, 0, s_>>>(dev_sys_, nslots_, counters_ + kOffActive);
+  k_bcount<<<1, 256, 0, s_>>>(dev_sys_, nslots_, counters_ + kOffActive, pending_, counters_ + kOffPending);
   count_launches(1);
   MGB_CUDA(cudaGetLastError());
   return MGB_OK;

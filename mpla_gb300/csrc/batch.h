@@ -18,7 +18,7 @@ struct BatchLane {
   double res;       // last stopping measure: ||r|| / ||b||
   int k;            // iterations done
   int done;         // 0 running, 1 converged, 2 capped, 3 broke down
-  int flag;         // mixed: FP64 true residual due this iteration
+  int hi;           // mixed: 0 iterating, 1 waiting for a true-residual round, 2 in the current round
   int replacements; // mixed: FP64 true residuals computed
 };
 
@@ -30,12 +30,15 @@ struct BatchSys {
   int precision;     // MGB_PREC_FP64 or MGB_PREC_MIXED
   int iter_max;
   int active_lanes;  // lanes still running (updated at the end of a step)
-  int need_hi;       // mixed: some lane needs the FP64 true residual this step
+  int live_lanes;    // running lanes not waiting for a true residual (end of a step)
+  int hi_step;       // mixed: steps of the current true-residual round done (-1: no round)
+  int hi_ready;      // mixed: the round's sums are complete; its lanes are replaced this step
+  int nstream;       // mixed: column streams of a true-residual round
   int nchunks;       // column chunks of the matvec items
   int nvec;          // row chunks of the vector phases
-  int pad;
   double eps, nugget;
   double *x, *r, *d, *z, *b;
+  double* zt;            // mixed: true-residual sums, nstream x n x R double-double (hi, lo)
   double* P;             // matvec partials: nchunks x n x R (chunk-major)
   double* vpart;         // vector-phase partial sums: nvec x 8
   unsigned int* ticket;  // last-arrival counter of the vector phases
@@ -62,12 +65,11 @@ class BatchEngine {
  public:
   static constexpr int kClasses = 8;        // (dim 2|3) x (R 1|2|4|8)
   static constexpr int kStepsPerGraph = 8;  // CG iterations per graph replay
-  static constexpr int kBranches = 2 * kClasses;  // concurrent matvec launches of a phase
+  static constexpr int kBranches = 3 * kClasses;  // concurrent launches of the matvec phase
   // Matvec item lists per class: every item (FP64 matvecs), the items whose
   // row tile is even / a multiple of 4 (FP32 variants with 2 / 4 rows per
-  // thread cover 2 / 4 consecutive row tiles), the chunk-0 items (whole-row
-  // true residuals).
-  static constexpr int kListAll = 0, kListRpt2 = 1, kListRpt4 = 2, kListTrue = 3, kLists = 4;
+  // thread cover 2 / 4 consecutive row tiles).
+  static constexpr int kListAll = 0, kListRpt2 = 1, kListRpt4 = 2, kLists = 3;
   // device counters: matvec queues (claim, finished) per class and mode,
   // item counts per list and class, the active-system count, vector-phase
   // queues (claim, finished) per phase and the vector item count
@@ -76,7 +78,8 @@ class BatchEngine {
   static constexpr int kOffActive = kOffCount + kLists * kClasses;
   static constexpr int kOffVec = kOffActive + 1;
   static constexpr int kOffVecCount = kOffVec + 8;
-  static constexpr int kCounterInts = kOffVecCount + 4;
+  static constexpr int kOffPending = kOffVecCount + 4;  // systems with a true-residual round in progress
+  static constexpr int kCounterInts = kOffPending + 4;
 
   ~BatchEngine();
   int init(DeviceContext* c, int max_systems, cudaStream_t s);
@@ -103,6 +106,7 @@ class BatchEngine {
   int join_branches(int nb);
   int enqueue_mv32(int cls, int rpt, cudaStream_t s);
   int enqueue_mv64(int cls, int mode, cudaStream_t s);
+  int enqueue_true(int cls, cudaStream_t s);
   int enqueue_vec(int phase);
 
   DeviceContext* c_ = nullptr;
@@ -121,6 +125,7 @@ class BatchEngine {
   bool has_mixed_[kClasses] = {};  // classes holding mixed / FP64 systems
   bool has_fp64_[kClasses] = {};
   VecItem* vitems_ = nullptr;
+  int* pending_ = nullptr;  // slots with a true-residual round in progress (device, slot order)
   std::vector<VecItem> vitems_host_;
   int vcount_host_ = 0;
   int max_items_ = 0;

@@ -38,6 +38,7 @@
 //   coordinates pre-scaled by sqrt(log2 e)).  About 8 issue slots and 1 MUFU
 //   per evaluated entry.
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <numeric>
@@ -289,7 +290,7 @@ __device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
 constexpr int kGroup = 4;
 constexpr double kFarLog2 = 40.0;
 
-template <int DIM>
+template <int DIM, bool SCALAR>
 __global__ void __launch_bounds__(kF32Threads) sym_f32_group_kernel(int n, int T, int GT,
                                                                     const int2* __restrict__ map,
                                                                     const float4* __restrict__ pts,
@@ -336,27 +337,61 @@ __global__ void __launch_bounds__(kF32Threads) sym_f32_group_kernel(int n, int T
     }
 #pragma unroll
     for (int b = 0; b < 32; ++b) {
-      const ulonglong2 q2 = cq[32 * warp + b];
-      const ulonglong2 w2 = cw[32 * warp + b];
-      const uint64_t qx = q2.x, qy = q2.y, qz = w2.x, qw = w2.y;
+      uint64_t qx, qy, qz, qw;
+      float qxs = 0.f, qys = 0.f;
+      if (SCALAR && DIM <= 2) {
+        // one 16-byte load {x, x, y, y}: the scalar coordinates, and {x_t, x_t}
+        const float4 q4 = reinterpret_cast<const float4*>(cq)[32 * warp + b];
+        qxs = q4.x;
+        qys = q4.z;
+        qx = qy = qz = 0ull;
+        qw = reinterpret_cast<const ulonglong2*>(cw)[32 * warp + b].y;
+      } else {
+        const ulonglong2 q2 = cq[32 * warp + b];
+        const ulonglong2 w2 = cw[32 * warp + b];
+        qx = q2.x;
+        qy = q2.y;
+        qz = w2.x;
+        qw = w2.y;
+      }
       uint64_t c2 = f2_pack(col[b], 0.f);
 #pragma unroll
       for (int q = 0; q < 2; ++q) {
-        const uint64_t dx = f2_sub(rx[q], qx);
-        uint64_t s2;
-        if (DIM == 1) {
-          s2 = f2_mul(dx, dx);
-        } else if (DIM == 2) {
-          const uint64_t dy = f2_sub(ry[q], qy);
-          s2 = f2_fma(dx, dx, f2_mul(dy, dy));
+        float ns0, ns1;  // minus the squared distances of the two rows
+        if (SCALAR && DIM <= 2) {
+          // scalar FP32 with the negation folded into the FMA: fewer
+          // registers and no repacking between the packed and scalar forms
+          float ax, bx, ay, by;
+          f2_unpack(rx[q], ax, bx);
+          const float dxa = ax - qxs, dxb = bx - qxs;
+          if (DIM == 1) {
+            ns0 = -dxa * dxa;
+            ns1 = -dxb * dxb;
+          } else {
+            f2_unpack(ry[q], ay, by);
+            const float dya = ay - qys, dyb = by - qys;
+            ns0 = fmaf(-dxa, dxa, -(dya * dya));
+            ns1 = fmaf(-dxb, dxb, -(dyb * dyb));
+          }
         } else {
-          const uint64_t dy = f2_sub(ry[q], qy);
-          const uint64_t dz = f2_sub(rz[q], qz);
-          s2 = f2_fma(dx, dx, f2_fma(dy, dy, f2_mul(dz, dz)));
+          const uint64_t dx = f2_sub(rx[q], qx);
+          uint64_t s2;
+          if (DIM == 1) {
+            s2 = f2_mul(dx, dx);
+          } else if (DIM == 2) {
+            const uint64_t dy = f2_sub(ry[q], qy);
+            s2 = f2_fma(dx, dx, f2_mul(dy, dy));
+          } else {
+            const uint64_t dy = f2_sub(ry[q], qy);
+            const uint64_t dz = f2_sub(rz[q], qz);
+            s2 = f2_fma(dx, dx, f2_fma(dy, dy, f2_mul(dz, dz)));
+          }
+          float s0, s1;
+          f2_unpack(s2, s0, s1);
+          ns0 = -s0;
+          ns1 = -s1;
         }
-        float s0, s1;
-        f2_unpack(s2, s0, s1);
-        const uint64_t e2 = f2_pack(ex2_approx(-s0), ex2_approx(-s1));
+        const uint64_t e2 = f2_pack(ex2_approx(ns0), ex2_approx(ns1));
         acc[q] = f2_fma(e2, qw, acc[q]);
         c2 = f2_fma(e2, xi2[q], c2);
       }
@@ -616,10 +651,19 @@ int SymF32::init(DeviceContext* c, const GaussSystem& g, cudaStream_t s) {
 int SymF32::apply(const double* x, double* y, cudaStream_t s, const int* skip) {
   sym_f32_gather_kernel<<<(n_ + 255) / 256, 256, 0, s>>>(n_, perm_, x, xf_, skip);
   const unsigned grid = (unsigned)ncta_;
-  switch (dim_) {
-    case 1: sym_f32_group_kernel<1><<<grid, kF32Threads, 0, s>>>(n_, T_, GT_, map_, pts_, xf_, S_, Scol_, skip); break;
-    case 2: sym_f32_group_kernel<2><<<grid, kF32Threads, 0, s>>>(n_, T_, GT_, map_, pts_, xf_, S_, Scol_, skip); break;
-    default: sym_f32_group_kernel<3><<<grid, kF32Threads, 0, s>>>(n_, T_, GT_, map_, pts_, xf_, S_, Scol_, skip); break;
+  static const int variant = getenv("MGB_GROUP_VARIANT") ? atoi(getenv("MGB_GROUP_VARIANT")) : 0;
+  if (variant == 1) {
+    switch (dim_) {
+      case 1: sym_f32_group_kernel<1, true><<<grid, kF32Threads, 0, s>>>(n_, T_, GT_, map_, pts_, xf_, S_, Scol_, skip); break;
+      case 2: sym_f32_group_kernel<2, true><<<grid, kF32Threads, 0, s>>>(n_, T_, GT_, map_, pts_, xf_, S_, Scol_, skip); break;
+      default: sym_f32_group_kernel<3, true><<<grid, kF32Threads, 0, s>>>(n_, T_, GT_, map_, pts_, xf_, S_, Scol_, skip); break;
+    }
+  } else {
+    switch (dim_) {
+      case 1: sym_f32_group_kernel<1, false><<<grid, kF32Threads, 0, s>>>(n_, T_, GT_, map_, pts_, xf_, S_, Scol_, skip); break;
+      case 2: sym_f32_group_kernel<2, false><<<grid, kF32Threads, 0, s>>>(n_, T_, GT_, map_, pts_, xf_, S_, Scol_, skip); break;
+      default: sym_f32_group_kernel<3, false><<<grid, kF32Threads, 0, s>>>(n_, T_, GT_, map_, pts_, xf_, S_, Scol_, skip); break;
+    }
   }
   sym_f32_reduce_kernel<<<(n_ + 255) / 256, 256, 0, s>>>(n_, T_, GT_, S_, Scol_, near_off_, near_J_, perm_, x,
                                                           nugget_, y, skip);

@@ -157,6 +157,30 @@ def bicgstab(op, b, x0=None, iter_max=1000, eps=1e-10, history=False):
     return out + (hist,) if history else out
 
 
+_PRIMES = (2, 3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 37, 41, 43, 47, 53)
+
+
+def halton(n: int, dim: int, start: int = 0) -> np.ndarray:
+    """Halton points (dim x n): coordinate d of point i is the radical inverse
+    of start + i + 1 in the d-th prime base, digits least significant first,
+    f *= 1/base per digit (the operation order of the library).  The point
+    set of generate_quadrature_weights.cpp:107-130, whose GSL generator is
+    not available here: this restates the published definition."""
+    out = np.empty((dim, n))
+    for d in range(dim):
+        base = _PRIMES[d]
+        inv = 1.0 / base
+        k = np.arange(start + 1, start + n + 1, dtype=np.int64)
+        f = np.full(n, inv)
+        x = np.zeros(n)
+        while np.any(k > 0):
+            x = x + f * (k % base).astype(np.float64)
+            k = k // base
+            f = f * inv
+        out[d] = x
+    return out
+
+
 def true_relres(op, b, x) -> float:
     b, x = _f64(b), _f64(x)
     return lib().orc_true_relres(C.byref(op.op), b.ctypes.data, x.ctypes.data)

@@ -11,6 +11,7 @@ that ends by itself (a few hundred MB on the device at most):
   python profile_cases.py batch128    # 16 timed steps of 128 batch systems (n <= 16384)
   python profile_cases.py batch128_solve  # the same 128 systems solved to 1e-10
   python profile_cases.py mixed_c3    # full mixed solve, n = 131072, d = 3, l = 0.08
+  python profile_cases.py batch_trace # all 512 batch systems to 1e-10, per-replay times
   python profile_cases.py all
 
 Prints the CUDA-event time per launch of each case.
@@ -52,7 +53,7 @@ def case_gauss_f64(reps=2):
     _gauss(16384, 2, 0.05, mg.PREC_FP64, reps)
 
 
-def case_gauss_mixed(reps=3):
+def case_gauss_mixed(reps=20):
     _gauss(65536, 2, 0.05, mg.PREC_MIXED, reps)
 
 
@@ -134,6 +135,49 @@ def case_batch128_solve():
     batch.close()
 
 
+def case_batch_trace(count=512, out="gpurun_out/batch_trace.csv"):
+    """All `count` systems of the batch workload admitted together and run to
+    relres 1e-10 one graph replay (8 steps) at a time: per replay the host
+    wall time and the systems still running (a CSV), then the total, the
+    replay-time distribution and the slowest systems."""
+    import time
+
+    spec = synth.batch_spec(512)
+    batch = mg.Batch(count)
+    handles = []
+    for k in range(count):
+        g = synth.batch_system(spec, k)
+        handles.append((k, batch.add(g.scaled(), g.nugget, g.b, precision=mg.PREC_MIXED, iter_max=300000)))
+    batch.run(max_steps=0)
+    rows = []
+    t0 = time.perf_counter()
+    active = count
+    while active > 0:
+        t = time.perf_counter()
+        active = batch.run(max_steps=8)
+        rows.append((len(rows), time.perf_counter() - t, active))
+    sec = time.perf_counter() - t0
+    Path(out).parent.mkdir(parents=True, exist_ok=True)
+    with open(out, "w") as f:
+        f.write("replay,seconds,active\n")
+        for r in rows:
+            f.write(f"{r[0]},{r[1]:.6f},{r[2]}\n")
+    dts = np.array([r[1] for r in rows])
+    res = []
+    for k, h in handles:
+        n, r = int(spec.n[k]), int(spec.nrhs[k])
+        _, infos = batch.result(h, n, r)
+        res.append((max(i.iterations for i in infos), sum(i.fp64_matvecs for i in infos), n, int(spec.dim[k]),
+                    float(spec.ell[k]), r))
+    res.sort(reverse=True)
+    print(f"batch_trace {count}: {sec:.2f} s over {len(rows)} replays; replay ms p50 {np.median(dts) * 1e3:.2f}, "
+          f"p90 {np.percentile(dts, 90) * 1e3:.2f}, max {dts.max() * 1e3:.2f}; the slowest 10 % of replays take "
+          f"{np.sort(dts)[-max(1, len(dts) // 10):].sum():.2f} s; FP64 true residuals {sum(x[1] for x in res)}")
+    for it, rep, n, d, ell, r in res[:10]:
+        print(f"  n={n} d={d} l={ell:.3f} nrhs={r}: {it} iterations, {rep} FP64 true residuals (all lanes)")
+    batch.close()
+
+
 def case_mixed_c3():
     """The mixed-precision configuration: n = 131072 points U[0,1]^3, l = 0.08,
     nugget 1e-4, b = sin(2 pi x1) cos(2 pi x2), solved to relres 1e-10."""
@@ -158,12 +202,12 @@ def case_mixed_c3():
 
 CASES = {"dgemv": case_dgemv, "gauss_f64": case_gauss_f64, "gauss_mixed": case_gauss_mixed,
          "mixed_cg": case_mixed_cg, "batch": case_batch, "batch128": case_batch128,
-         "batch128_solve": case_batch128_solve, "mixed_c3": case_mixed_c3}
+         "batch128_solve": case_batch128_solve, "mixed_c3": case_mixed_c3, "batch_trace": case_batch_trace}
 
 
 def main(argv):
     mg.init(0)
-    long_cases = ("mixed_c3", "batch128", "batch128_solve")
+    long_cases = ("mixed_c3", "batch128", "batch128_solve", "batch_trace")
     names = [k for k in CASES if k not in long_cases] if (not argv or argv[0] == "all") else argv
     for name in names:
         CASES[name]()

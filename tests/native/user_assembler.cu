@@ -92,7 +92,7 @@ int main(int argc, char** argv) {
   cudaMemcpy(dpoints, cols.data(), sizeof(double*) * dim, cudaMemcpyHostToDevice);
   imq_system_assembler** dobj = nullptr;
   cudaMalloc((void**)&dobj, sizeof(*dobj));
-  create_imq<<<1, 1>>>(dobj, dpoints, dim, 0.25, 0.5);
+  create_imq<<<1, 1>>>(dobj, dpoints, dim, 0.25, 5.0);
   imq_system_assembler* obj = nullptr;
   cudaMemcpy(&obj, dobj, sizeof(obj), cudaMemcpyDeviceToHost);
   checkCUDAError("create_imq");

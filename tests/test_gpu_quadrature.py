@@ -1,0 +1,80 @@
+"""The quadrature-weight application on the GB300 library against the oracle.
+
+mpla_gb300/apps/generate_quadrature_weights.cpp follows MPLA's
+generate_quadrature_weights.cpp:18-173 through the mpla.h API: Halton points,
+kernel_matrix_data with the streamed kernel core (exp(-r^2), +1e-8 where
+r < 1e-14), b from mpla_set_gaussian_kernel_rhs (the integrals of the kernel
+over the unit cube), a uniform random start vector, the checkpointing CG to
+relative tolerance 1e-7, weights.dat in MPLA's vector format.  The oracle
+runs its CG (mpla.cpp:887-1001 restated) on the same points, right-hand side
+and start vector.  This system is ill-conditioned (only the 1e-8 diagonal
+regularises it), so the iteration counts agree within 3 %, like the other
+ill-conditioned kernel family; the weights reach the tolerance on the FP64
+oracle operator and integrate test functions like the oracle's weights.
+"""
+import os
+import re
+import shutil
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from mpla_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+ROOT = Path(__file__).resolve().parents[1]
+CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
+
+
+@pytest.fixture(scope="module")
+def app(gpu, tmp_path_factory):
+    import mpla_gb300
+
+    out = tmp_path_factory.mktemp("quadrature") / "generate_quadrature_weights"
+    libdir = mpla_gb300.LIB_PATH.parent
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", "-I", str(ROOT / "include"), "-I", str(CUDA_HOME / "include"),
+           str(ROOT / "mpla_gb300" / "apps" / "generate_quadrature_weights.cpp"), "-o", str(out),
+           "-L", str(libdir), f"-Wl,-rpath,{libdir}", "-lmpla",
+           "-L", str(CUDA_HOME / "lib64"), f"-Wl,-rpath,{CUDA_HOME / 'lib64'}", "-lcudart"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    assert res.returncode == 0, res.stdout + res.stderr
+    return out
+
+
+def run(app, cwd, *args):
+    res = subprocess.run([str(app), *map(str, args)], capture_output=True, text=True, cwd=cwd, timeout=600)
+    assert res.returncode == 0, res.stdout + res.stderr
+    m = re.search(r"stopped after (\d+) iterations", res.stdout)
+    assert m and "Time spent:" in res.stdout, res.stdout
+    return int(m.group(1)), res.stdout
+
+
+def test_quadrature_weights_match_oracle_with_checkpoint_restart(app, orc, tmp_path):
+    n, dim, tol = 1000, 3, 1e-7
+    k, out = run(app, tmp_path, n, dim, tol, 0, 200)
+    assert "Checkpointing..." in out
+    st, w = orc.load_vector(str(tmp_path / "weights.dat"), n)
+    assert st == 0
+
+    pts = orc.halton(n, dim)
+    op = orc.GaussOp(pts, 0.0, rule=orc.RULE_KERNEL_CU)
+    b = op.rhs()
+    x0 = synth.uniform(1235, 1, n)
+    w_orc, k_orc, _, st_orc = orc.cg(op, b, x0, iter_max=100000, eps=tol)
+    assert st_orc == 0
+    assert abs(k - k_orc) <= 0.03 * k_orc, (k, k_orc)
+    assert orc.true_relres(op, b, w) < 2 * tol
+    # weights integrate over [0,1]^3: 1 and x1 x2 x3 (1/8) like the oracle's
+    for f in (np.ones(n), pts[0] * pts[1] * pts[2]):
+        assert abs(f @ w - f @ w_orc) < 1e-5
+
+    # restart from the checkpoint files of the first run (x, r, d, z)
+    k2, _ = run(app, tmp_path, n, dim, tol, 1, 200)
+    st, w2 = orc.load_vector(str(tmp_path / "weights.dat"), n)
+    assert st == 0
+    assert orc.true_relres(op, b, w2) < 2 * tol
+    assert abs(np.sum(w2) - np.sum(w)) < 1e-5

@@ -157,3 +157,18 @@ def test_oracle_accurate_residual_is_exact_where_plain_fp64_is_not(orc):
     b = np.concatenate([np.ones(n), [0.0]])
     assert orc.true_relres_accurate(op, b, x) == 0.0
     assert orc.true_relres(op, b, x) > 1e-3
+
+
+def test_halton_library_matches_oracle_restatement(native_lib):
+    """mgb_halton (host code) against the oracle's restatement, bit for bit,
+    and the first points against the definition (radical inverse in the
+    prime bases 2, 3, 5)."""
+    import mpla_gb300
+    import oracle
+
+    for n, dim, start in [(1000, 3, 0), (257, 16, 9), (4096, 2, 123456)]:
+        assert np.array_equal(mpla_gb300.halton(n, dim, start), oracle.halton(n, dim, start))
+    first = mpla_gb300.halton(4, 3)
+    assert np.allclose(first[0], [1 / 2, 1 / 4, 3 / 4, 1 / 8], rtol=0, atol=1e-15)
+    assert np.allclose(first[1], [1 / 3, 2 / 3, 1 / 9, 4 / 9], rtol=0, atol=1e-15)
+    assert np.allclose(first[2], [1 / 5, 2 / 5, 3 / 5, 4 / 5], rtol=0, atol=1e-15)
