@@ -38,7 +38,6 @@
 //   coordinates pre-scaled by sqrt(log2 e)).  About 8 issue slots and 1 MUFU
 //   per evaluated entry.
 #include <algorithm>
-#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <numeric>
@@ -287,6 +286,11 @@ __device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
 // the nugget.  The CTA map lists only groups with a near row tile, and a
 // 4-bit mask per CTA marks which of its row tiles are near; the slots of
 // far pairs are zeroed once and never written.
+//
+// SCALAR (d <= 2): the squared distance in scalar FP32 with the negation
+// folded into the FMA, the column values read as scalars from the same
+// staging; fewer registers (94 against 102) and no repacking between the
+// packed and scalar forms around the MUFU.EX2 operands.
 constexpr int kGroup = 4;
 constexpr double kFarLog2 = 40.0;
 
@@ -651,19 +655,12 @@ int SymF32::init(DeviceContext* c, const GaussSystem& g, cudaStream_t s) {
 int SymF32::apply(const double* x, double* y, cudaStream_t s, const int* skip) {
   sym_f32_gather_kernel<<<(n_ + 255) / 256, 256, 0, s>>>(n_, perm_, x, xf_, skip);
   const unsigned grid = (unsigned)ncta_;
-  static const int variant = getenv("MGB_GROUP_VARIANT") ? atoi(getenv("MGB_GROUP_VARIANT")) : 0;
-  if (variant == 1) {
-    switch (dim_) {
-      case 1: sym_f32_group_kernel<1, true><<<grid, kF32Threads, 0, s>>>(n_, T_, GT_, map_, pts_, xf_, S_, Scol_, skip); break;
-      case 2: sym_f32_group_kernel<2, true><<<grid, kF32Threads, 0, s>>>(n_, T_, GT_, map_, pts_, xf_, S_, Scol_, skip); break;
-      default: sym_f32_group_kernel<3, true><<<grid, kF32Threads, 0, s>>>(n_, T_, GT_, map_, pts_, xf_, S_, Scol_, skip); break;
-    }
-  } else {
-    switch (dim_) {
-      case 1: sym_f32_group_kernel<1, false><<<grid, kF32Threads, 0, s>>>(n_, T_, GT_, map_, pts_, xf_, S_, Scol_, skip); break;
-      case 2: sym_f32_group_kernel<2, false><<<grid, kF32Threads, 0, s>>>(n_, T_, GT_, map_, pts_, xf_, S_, Scol_, skip); break;
-      default: sym_f32_group_kernel<3, false><<<grid, kF32Threads, 0, s>>>(n_, T_, GT_, map_, pts_, xf_, S_, Scol_, skip); break;
-    }
+  // d <= 2: squared distances in scalar FP32 (5 % faster than the packed
+  // form at n = 65536, d = 2 on GB300: 0.288 against 0.304 ms); d = 3: packed
+  switch (dim_) {
+    case 1: sym_f32_group_kernel<1, true><<<grid, kF32Threads, 0, s>>>(n_, T_, GT_, map_, pts_, xf_, S_, Scol_, skip); break;
+    case 2: sym_f32_group_kernel<2, true><<<grid, kF32Threads, 0, s>>>(n_, T_, GT_, map_, pts_, xf_, S_, Scol_, skip); break;
+    default: sym_f32_group_kernel<3, false><<<grid, kF32Threads, 0, s>>>(n_, T_, GT_, map_, pts_, xf_, S_, Scol_, skip); break;
   }
   sym_f32_reduce_kernel<<<(n_ + 255) / 256, 256, 0, s>>>(n_, T_, GT_, S_, Scol_, near_off_, near_J_, perm_, x,
                                                           nugget_, y, skip);

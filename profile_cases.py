@@ -12,6 +12,7 @@ that ends by itself (a few hundred MB on the device at most):
   python profile_cases.py batch128_solve  # the same 128 systems solved to 1e-10
   python profile_cases.py mixed_c3    # full mixed solve, n = 131072, d = 3, l = 0.08
   python profile_cases.py batch_trace # all 512 batch systems to 1e-10, per-replay times
+  python profile_cases.py batch512    # 16 timed steps of all 512 batch systems
   python profile_cases.py all
 
 Prints the CUDA-event time per launch of each case.
@@ -103,6 +104,25 @@ def case_batch128(steps=16):
     rpt, tune = batch.tuning()
     print(f"batch128: {ms:.3f} ms per step, {active} of 128 systems running, rows per thread {rpt}, "
           f"FP32 matvec ms per class (2 / 4 rows per thread) {[[round(t, 4) for t in c[1:]] for c in tune]}")
+    batch.close()
+
+
+def case_batch512(steps=16):
+    """All 512 batch systems admitted together: one warm-up replay, then
+    `steps` iterations (the busiest step of the batch workload, for launch
+    lists)."""
+    import time
+
+    spec = synth.batch_spec(512)
+    batch = mg.Batch(512)
+    for k in range(512):
+        g = synth.batch_system(spec, k)
+        batch.add(g.scaled(), g.nugget, g.b, precision=mg.PREC_MIXED, iter_max=300000)
+    batch.run(max_steps=8)
+    t0 = time.perf_counter()
+    active = batch.run(max_steps=steps)
+    ms = (time.perf_counter() - t0) * 1e3 / steps
+    print(f"batch512: {ms:.3f} ms per step, {active} of 512 systems running")
     batch.close()
 
 
@@ -202,12 +222,13 @@ def case_mixed_c3():
 
 CASES = {"dgemv": case_dgemv, "gauss_f64": case_gauss_f64, "gauss_mixed": case_gauss_mixed,
          "mixed_cg": case_mixed_cg, "batch": case_batch, "batch128": case_batch128,
-         "batch128_solve": case_batch128_solve, "mixed_c3": case_mixed_c3, "batch_trace": case_batch_trace}
+         "batch128_solve": case_batch128_solve, "mixed_c3": case_mixed_c3, "batch_trace": case_batch_trace,
+         "batch512": case_batch512}
 
 
 def main(argv):
     mg.init(0)
-    long_cases = ("mixed_c3", "batch128", "batch128_solve", "batch_trace")
+    long_cases = ("mixed_c3", "batch128", "batch128_solve", "batch_trace", "batch512")
     names = [k for k in CASES if k not in long_cases] if (not argv or argv[0] == "all") else argv
     for name in names:
         CASES[name]()
