@@ -7,10 +7,13 @@ r < 1e-14), b from mpla_set_gaussian_kernel_rhs (the integrals of the kernel
 over the unit cube), a uniform random start vector, the checkpointing CG to
 relative tolerance 1e-7, weights.dat in MPLA's vector format.  The oracle
 runs its CG (mpla.cpp:887-1001 restated) on the same points, right-hand side
-and start vector.  This system is ill-conditioned (only the 1e-8 diagonal
-regularises it), so the iteration counts agree within 3 %, like the other
-ill-conditioned kernel family; the weights reach the tolerance on the FP64
-oracle operator and integrate test functions like the oracle's weights.
+and start vector.  This system is ill-conditioned (kappa = 6.5e10: only the
+1e-8 diagonal regularises it), and its FP64 CG count is not a stable
+quantity: the oracle needs 665 iterations, and 655 to 889 after relative
+perturbations of K by 1.1e-16 (a CPU measurement with the oracle), so the
+counts are compared within that spread (a factor 1.5).  The parity checks
+are on the results: the weights reach the tolerance on the FP64 oracle
+operator and integrate test functions like the oracle's weights.
 """
 import os
 import re
@@ -66,7 +69,7 @@ def test_quadrature_weights_match_oracle_with_checkpoint_restart(app, orc, tmp_p
     x0 = synth.uniform(1235, 1, n)
     w_orc, k_orc, _, st_orc = orc.cg(op, b, x0, iter_max=100000, eps=tol)
     assert st_orc == 0
-    assert abs(k - k_orc) <= 0.03 * k_orc, (k, k_orc)
+    assert k_orc / 1.5 <= k <= 1.5 * k_orc, (k, k_orc)
     assert orc.true_relres(op, b, w) < 2 * tol
     # weights integrate over [0,1]^3: 1 and x1 x2 x3 (1/8) like the oracle's
     for f in (np.ones(n), pts[0] * pts[1] * pts[2]):

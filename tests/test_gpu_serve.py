@@ -18,8 +18,8 @@ from mpla_gb300.serve import Request, Server, latency_stats, poisson_arrivals
 pytestmark = pytest.mark.gpu
 
 
-def make_request(k, arrival, rng):
-    n = int(np.exp(rng.uniform(np.log(300), np.log(1500))))
+def make_request(k, arrival, rng, n=None):
+    n = n or int(np.exp(rng.uniform(np.log(300), np.log(1500))))
     dim = 2 + int(rng.random() < 0.5)
     ell = float(rng.uniform(0.03, 0.2))
     r = int(rng.integers(1, 5))
@@ -33,6 +33,9 @@ def test_served_results_are_correct_and_match_solo_solves(gpu, orc):
     arrivals = poisson_arrivals(12.0, 1.0, rng)
     t0 = time.perf_counter()
     reqs = [make_request(k, t0 + a, rng) for k, a in enumerate(arrivals)]
+    # one mixed and one FP64 request of the serving configuration's larger
+    # sizes, arriving while the others run
+    reqs += [make_request(len(reqs) + j, t0 + 0.5, rng, n=8192 + 96 * j) for j in range(2)]
     batch = gpu.Batch(64)
     srv = Server(batch, slice_steps=32)
     for r in reqs:
