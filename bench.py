@@ -230,12 +230,21 @@ def bench_dense(mg, torch, stream, hbm_peak_gbs: float | None) -> dict:
 
 
 def bench_batched(mg, count: int) -> dict:
-    """Batched mixed-precision solves: `count` Gaussian systems (n log-uniform
-    in [256, 16384], d in {2,3}, l ~ U[0.03, 0.2], nugget 1e-4, 1-8 N(0,1)
-    right-hand sides), admitted together and run to relres 1e-10."""
+    """Batched mixed-precision solves: `count` Gaussian systems of the batch
+    workload (n log-uniform in [256, 16384], d in {2,3}, l ~ U[0.03, 0.2],
+    nugget 1e-4, 1-8 N(0,1) right-hand sides; 512 is the whole workload),
+    admitted together from host buffers and run to relres 1e-10.
+
+    Plain FP64 on the same systems is not run to the end (it would take tens
+    of minutes on GB300's FP64 pipe).  Its batch time is extrapolated from
+    three measurements: the mixed batch's wall time, the FP64 / mixed time
+    per step with every system running (16 steps each), and the FP64 / mixed
+    iteration ratio of the slowest right-hand side, measured by solving a
+    sample of the batch's systems (every system with n <= 2048, up to 24) to
+    the end in both precisions."""
     from mpla_gb300 import synth
 
-    spec = synth.batch_spec(512)  # the first `count` systems of the 512-system workload
+    spec = synth.batch_spec(512)
     systems = [synth.batch_system(spec, k) for k in range(count)]
     batch = mg.Batch(count)
     t_add0 = time.perf_counter()
@@ -250,25 +259,23 @@ def bench_batched(mg, count: int) -> dict:
     mg.synchronize()
     sec = time.perf_counter() - t0
     launches = mg.kernel_launches() - launches0
+    t_res0 = time.perf_counter()
     iters, statuses, worst = [], [], 0.0
     rhs_total = 0
-    for k, (h, g) in enumerate(zip(handles, systems)):
+    for h, g in zip(handles, systems):
         x, infos = batch.result(h, g.n, g.b.shape[1])
         rhs_total += g.b.shape[1]
         iters += [i.iterations for i in infos]
         statuses += [int(i.status) for i in infos]
         # each mixed lane's FP64 double-double true residual at convergence
         worst = max([worst] + [i.true_relres for i in infos])
+    t_res = time.perf_counter() - t_res0
     rpt, _ = batch.tuning()
     batch.close()
 
-    # plain FP64 against mixed on the same systems: a full FP64 batch would
-    # run for tens of minutes on GB300's FP64 pipe, so both precisions are
-    # timed over the same 16 steps at full occupancy (after an 8-step warm-up
-    # that also tunes and captures); FP64 CG needs ~0.75x the iterations
-    def ms_per_step(precision: int, steps: int = 16) -> float:
-        bt = mg.Batch(count)
-        for g in systems:
+    def ms_per_step(precision: int, subset, steps: int = 16) -> float:
+        bt = mg.Batch(len(subset))
+        for g in subset:
             bt.add(g.scaled(), g.nugget, g.b, precision=precision, eps=EPS, iter_max=300000)
         bt.run(max_steps=8)
         mg.synchronize()
@@ -279,66 +286,77 @@ def bench_batched(mg, count: int) -> dict:
         bt.close()
         return dt * 1e3
 
-    fp64_step, mixed_step = ms_per_step(mg.PREC_FP64), ms_per_step(mg.PREC_MIXED)
-    return {"workload": f"the first {count} of 512 Gaussian systems, n log-uniform [256,16384], d in {{2,3}}, "
+    def solve_iterations(precision: int, subset) -> list[int]:
+        bt = mg.Batch(len(subset))
+        hs = [bt.add(g.scaled(), g.nugget, g.b, precision=precision, eps=EPS, iter_max=300000) for g in subset]
+        bt.run()
+        out = [max(i.iterations for i in bt.result(h, g.n, g.b.shape[1])[1]) for h, g in zip(hs, subset)]
+        bt.close()
+        return out
+
+    fp64_step, mixed_step = ms_per_step(mg.PREC_FP64, systems), ms_per_step(mg.PREC_MIXED, systems)
+    sample = [g for g in systems if g.n <= 2048][:24]
+    k64, k32 = solve_iterations(mg.PREC_FP64, sample), solve_iterations(mg.PREC_MIXED, sample)
+    ratio_iters = float(sum(k64)) / float(sum(k32))
+    fp64_seconds_est = sec * (fp64_step / mixed_step) * ratio_iters
+    return {"workload": f"{count} of the 512 Gaussian systems, n log-uniform [256,16384], d in {{2,3}}, "
                         "l ~ U[0.03,0.2], nugget 1e-4, 1-8 N(0,1) right-hand sides, mixed precision, relres 1e-10",
             "systems_per_s": count / sec, "rhs_solves_per_s": rhs_total / sec, "seconds": sec,
-            "e2e_systems_per_s": count / (sec + t_add), "admission_seconds": t_add,
+            "e2e_systems_per_s": count / (sec + t_add + t_res), "admission_seconds": t_add,
+            "result_readback_seconds": t_res,
             "unfinished": left, "all_converged": all(s == 0 for s in statuses),
-            "iterations_median": float(np.median(iters)), "iterations_max": int(max(iters)),
+            "rhs_total": rhs_total, "iterations_median": float(np.median(iters)), "iterations_max": int(max(iters)),
             "worst_true_relres": worst, "gpu_launches": int(launches),
             "fp64_ms_per_step": fp64_step, "mixed_ms_per_step": mixed_step,
-            "mixed_over_fp64_per_step": fp64_step / mixed_step,
+            "fp64_over_mixed_per_step": fp64_step / mixed_step,
+            "fp64_over_mixed_iterations": ratio_iters,
+            "iteration_sample": f"{len(sample)} systems with n <= 2048 solved to the end in both precisions "
+                                f"(slowest right-hand side): FP64 {sum(k64)}, mixed {sum(k32)} iterations",
+            "fp64_systems_per_s_extrapolated": count / fp64_seconds_est,
+            "fp64_seconds_extrapolated": fp64_seconds_est,
+            "mixed_over_fp64_solves": fp64_seconds_est / sec,
+            "extrapolation": "FP64 batch time = mixed batch time x FP64/mixed time per step (all systems running) "
+                             "x FP64/mixed iterations (sample)",
             "autotuner_rows_per_thread": rpt}
 
 
-def bench_serving(mg, rate: float, window: float, drain: float, seed: int = 0) -> dict:
-    """Continuous batching: Poisson arrivals at `rate` per second for `window`
-    seconds; n log-uniform in [1024, 32768], d in {2,3}, l ~ U[0.03, 0.2],
-    1-4 N(0,1) right-hand sides, half FP64 and half mixed, relres 1e-10."""
+def bench_serving(mg, rates, per_rate: int, n_hi: int, drain: float, seed: int = 0) -> list:
+    """Continuous batching at several arrival rates: per rate, Poisson
+    arrivals over a window of per_rate / rate seconds (about `per_rate`
+    requests), n log-uniform in [1024, n_hi], d in {2,3}, l ~ U[0.03, 0.2],
+    1-4 N(0,1) right-hand sides, half FP64 and half mixed, relres 1e-10,
+    drained until every request has finished (or `drain` seconds)."""
     from mpla_gb300 import synth
-    from mpla_gb300.serve import Request, Server, latency_stats, poisson_arrivals
+    from mpla_gb300.serve import Request, Server, latency_stats
 
-    rng = np.random.default_rng(seed)
-    arrivals = poisson_arrivals(rate, window, rng)
-    reqs = []
-    for k, a in enumerate(arrivals):
-        n = int(np.exp(rng.uniform(np.log(1024), np.log(32768))))
-        dim = 2 + int(rng.random() < 0.5)
-        ell = float(rng.uniform(0.03, 0.2))
-        r = int(rng.integers(1, 5))
-        pts = np.stack([synth.uniform(seed, 5000 + 16 * k + j, n) for j in range(dim)]) / (math.sqrt(2.0) * ell)
-        b = np.stack([synth.normal(seed, 6_000_000 + 16 * k + j, n) for j in range(r)], axis=1)
-        reqs.append((a, k, pts, b))
-    batch = mg.Batch(256)
-    srv = Server(batch, slice_steps=64)
-    t0 = time.perf_counter()
-    for a, k, pts, b in reqs:
-        srv.submit(Request(arrival=t0 + a, rid=k, points=pts, b=b, precision=k % 2))
-    srv.serve(until=t0 + window, drain_until=t0 + window + drain)
-    t_end = time.perf_counter()
-    st = latency_stats(srv.done)
-    # requests still running at the drain deadline: their latency is at least
-    # the time they have waited, so percentiles over all requests with those
-    # lower bounds are lower bounds themselves
-    waited = [c.latency for c in srv.done] + [t_end - (t0 + a) for a, k, _, _ in reqs
-                                               if k not in {c.rid for c in srv.done}]
-    if waited:
-        st["p50_s_all_lower_bound"] = float(np.percentile(waited, 50))
-        st["p99_s_all_lower_bound"] = float(np.percentile(waited, 99))
-    conv = all(int(i.status) == 0 for c in srv.done for i in c.infos)
-    by_prec = {}
-    for p, name in ((0, "fp64"), (1, "mixed")):
-        lat = [c.latency for c in srv.done if c.precision == p]
-        if lat:
-            by_prec[name] = {"completed": len(lat), "p50_s": float(np.percentile(lat, 50)),
-                             "p99_s": float(np.percentile(lat, 99))}
-    batch.close()
-    st.update({"workload": f"Poisson arrivals {rate}/s for {window} s, n log-uniform [1024,32768], d in {{2,3}}, "
-                           "l ~ U[0.03,0.2], 1-4 N(0,1) right-hand sides, half FP64 / half mixed, relres 1e-10",
-               "submitted": len(reqs), "unfinished": len(reqs) - len(srv.done), "all_converged": conv,
-               "admission_refusals": srv.refusals, "by_precision": by_prec})
-    return st
+    out = []
+    for q, rate in enumerate(rates):
+        window = per_rate / rate
+        reqs = synth.serving_requests(rate, window, seed=seed + q, n_hi=n_hi)
+        batch = mg.Batch(256)
+        srv = Server(batch, slice_steps=64)
+        t0 = time.perf_counter()
+        for a, k, pts, b, prec in reqs:
+            srv.submit(Request(arrival=t0 + a, rid=k, points=pts, b=b, precision=prec))
+        srv.serve(until=t0 + window, drain_until=t0 + window + drain)
+        st = latency_stats(srv.done)
+        conv = all(int(i.status) == 0 for c in srv.done for i in c.infos)
+        by_prec = {}
+        for p, name in ((0, "fp64"), (1, "mixed")):
+            lat = [c.latency for c in srv.done if c.precision == p]
+            if lat:
+                by_prec[name] = {"completed": len(lat), "p50_s": float(np.percentile(lat, 50)),
+                                 "p99_s": float(np.percentile(lat, 99)),
+                                 "n_max": int(max(c.n for c in srv.done if c.precision == p))}
+        batch.close()
+        st.update({"rate_per_s": rate, "window_s": window,
+                   "workload": f"Poisson arrivals {rate}/s for {window:g} s, n log-uniform [1024,{n_hi}], "
+                               "d in {2,3}, l ~ U[0.03,0.2], 1-4 N(0,1) right-hand sides, half FP64 / half mixed, "
+                               "relres 1e-10",
+                   "submitted": len(reqs), "unfinished": len(reqs) - len(srv.done), "all_converged": conv,
+                   "admission_refusals": srv.refusals, "by_precision": by_prec})
+        out.append(st)
+    return out
 
 
 # ---------------------------------------------------------------- our arm
@@ -462,7 +480,8 @@ def run_ours(args, world, rank, local):
         extra["batched"] = bench_batched(mg, args.batch_systems)
         progress("batched done")
     if not args.no_serving:
-        extra["serving"] = bench_serving(mg, args.serve_rate, args.serve_window, args.serve_drain)
+        extra["serving"] = bench_serving(mg, [float(r) for r in args.serve_rates.split(",")], args.serve_per_rate,
+                                         args.serve_n_max, args.serve_drain)
         progress("serving done")
     cpu = cpu_baseline(pts_scaled, NUGGET, iters_fp64, budget_s=args.cpu_seconds) if not args.no_cpu else None
     line = {
@@ -631,11 +650,14 @@ def main(argv=None):
     p.add_argument("--no-dense", action="store_true")
     p.add_argument("--no-batched", action="store_true")
     p.add_argument("--no-serving", action="store_true")
-    p.add_argument("--batch-systems", type=int, default=128,
-                   help="systems of the 512-system batch workload to run (a prefix: 512 runs all of it)")
-    p.add_argument("--serve-rate", type=float, default=1.0)
-    p.add_argument("--serve-window", type=float, default=5.0)
-    p.add_argument("--serve-drain", type=float, default=60.0)
+    p.add_argument("--batch-systems", type=int, default=512,
+                   help="systems of the 512-system batch workload to run (a prefix; 512 is all of it)")
+    p.add_argument("--serve-rates", default="0.5,1,2", help="arrival rates per second, comma-separated")
+    p.add_argument("--serve-per-rate", type=int, default=8, help="expected requests per rate")
+    p.add_argument("--serve-n-max", type=int, default=8192,
+                   help="largest request size (the serving configuration's 32768 makes single FP64 requests run "
+                        "for minutes on GB300's FP64 pipe; the full sweep is profile_cases.py serving_sweep)")
+    p.add_argument("--serve-drain", type=float, default=300.0)
     args = p.parse_args(argv)
     if args.warmup < 3:
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

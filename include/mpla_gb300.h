@@ -212,8 +212,12 @@ int mgb_batch_finished(mgb_batch* b, int* handles, int capacity, int* count);
 /* Copy x (column-major, n x nrhs) and one mgb_solve_info per right-hand side
  * to the host; release != 0 frees the slot and its device memory. */
 int mgb_batch_result(mgb_batch* b, int handle, double* x_host, mgb_solve_info* info, int release);
-/* Autotuner choice per (dimension, padded right-hand sides) class:
- * rows_per_thread[8] and the timed ms of the 1/2/4 variants (ms[24]). */
+/* Systems are grouped in classes by dimension (2, 3) and right-hand-side
+ * width R (nrhs, with 5 padded to 6 and 7 to 8): class = (dim == 3 ? 6 : 0)
+ * + position of R in {1, 2, 3, 4, 6, 8}.  Autotuner choice per class:
+ * rows_per_thread[MGB_BATCH_CLASSES] and the timed ms of the 1/2/4 variants
+ * (ms[3 * MGB_BATCH_CLASSES]). */
+#define MGB_BATCH_CLASSES 12
 int mgb_batch_tuning(mgb_batch* b, int* rows_per_thread, float* ms);
 int mgb_batch_destroy(mgb_batch* b);
 

@@ -34,6 +34,7 @@ PREC_FP64 = 0
 PREC_MIXED = 1
 MIXED_TENSOR = 0
 MIXED_SIMT = 1
+BATCH_CLASSES = 12  # MGB_BATCH_CLASSES
 
 # Every C-ABI symbol declared in include/mpla_gb300.h (checked by the tests).
 C_ABI_SYMBOLS = (
@@ -411,10 +412,12 @@ class Batch:
         return x.T.copy(), list(infos)
 
     def tuning(self):
-        rpt = (_I * 8)()
-        ms = (C.c_float * 24)()
+        """Per class (dim 2|3 x R 1|2|3|4|6|8): FP32 matvec rows per thread
+        chosen by the autotuner, and the timed ms of the 1/2/4 variants."""
+        rpt = (_I * BATCH_CLASSES)()
+        ms = (C.c_float * (3 * BATCH_CLASSES))()
         check(lib().mgb_batch_tuning(self._h, rpt, ms))
-        return list(rpt), [list(ms[3 * c:3 * c + 3]) for c in range(8)]
+        return list(rpt), [list(ms[3 * c:3 * c + 3]) for c in range(BATCH_CLASSES)]
 
     def close(self) -> None:
         if getattr(self, "_h", None):

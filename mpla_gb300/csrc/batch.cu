@@ -658,7 +658,9 @@ __global__ void __launch_bounds__(kVecThreads) k_bvec(WorkQueue q, const VecItem
     break;
       MGB_BVEC_CASE(1)
       MGB_BVEC_CASE(2)
+      MGB_BVEC_CASE(3)
       MGB_BVEC_CASE(4)
+      MGB_BVEC_CASE(6)
       MGB_BVEC_CASE(8)
 #undef MGB_BVEC_CASE
       default:
@@ -783,7 +785,9 @@ __global__ void __launch_bounds__(256) k_bcount(BatchSys* sys, int nslots, int* 
   if (threadIdx.x == 0) *npending = s_base;
 }
 
-int padded_rhs(int r) { return r <= 1 ? 1 : (r <= 2 ? 2 : (r <= 4 ? 4 : 8)); }
+// Right-hand-side widths with their own kernels: 5 runs as 6 and 7 as 8.
+int padded_rhs(int r) { return r <= 4 ? (r < 1 ? 1 : r) : (r <= 6 ? 6 : 8); }
+constexpr int kWidths[6] = {1, 2, 3, 4, 6, 8};
 
 }  // namespace
 
@@ -842,8 +846,9 @@ BatchEngine::~BatchEngine() {
 }
 
 int BatchEngine::class_of(int dim, int R) {
-  const int r = R == 1 ? 0 : (R == 2 ? 1 : (R == 4 ? 2 : 3));
-  return (dim == 2 ? 0 : 4) + r;
+  int r = 0;
+  while (r < 5 && kWidths[r] != R) ++r;
+  return (dim == 2 ? 0 : 6) + r;
 }
 
 static int chunks_of(int n) { return (n + kChunkCols - 1) / kChunkCols; }
@@ -1072,20 +1077,30 @@ static void launch_mv32(const WorkQueue& q, const BatchSys* sys, int rpt, int gr
   else k_bmv32<DIM, R, 2><<<grid, kTile, 0, s>>>(q, sys);
 }
 
+// class index -> (DIM, R) for the templated launches
+#define MGB_CLASS_SWITCH(cls, CALL)                 \
+  switch (cls) {                                    \
+    case 0: CALL(2, 1); break;                      \
+    case 1: CALL(2, 2); break;                      \
+    case 2: CALL(2, 3); break;                      \
+    case 3: CALL(2, 4); break;                      \
+    case 4: CALL(2, 6); break;                      \
+    case 5: CALL(2, 8); break;                      \
+    case 6: CALL(3, 1); break;                      \
+    case 7: CALL(3, 2); break;                      \
+    case 8: CALL(3, 3); break;                      \
+    case 9: CALL(3, 4); break;                      \
+    case 10: CALL(3, 6); break;                     \
+    default: CALL(3, 8); break;                     \
+  }
+
 int BatchEngine::enqueue_mv32(int cls, int rpt, cudaStream_t s) {
   const int list = rpt == 4 ? kListRpt4 : kListRpt2;
   const WorkQueue q = make_queue(items_[list][cls], counters_, cls, Q_MV32, list);
   const int grid = 4 * c_->num_sms;
-  switch (cls) {
-    case 0: launch_mv32<2, 1>(q, dev_sys_, rpt, grid, s); break;
-    case 1: launch_mv32<2, 2>(q, dev_sys_, rpt, grid, s); break;
-    case 2: launch_mv32<2, 4>(q, dev_sys_, rpt, grid, s); break;
-    case 3: launch_mv32<2, 8>(q, dev_sys_, rpt, grid, s); break;
-    case 4: launch_mv32<3, 1>(q, dev_sys_, rpt, grid, s); break;
-    case 5: launch_mv32<3, 2>(q, dev_sys_, rpt, grid, s); break;
-    case 6: launch_mv32<3, 4>(q, dev_sys_, rpt, grid, s); break;
-    default: launch_mv32<3, 8>(q, dev_sys_, rpt, grid, s); break;
-  }
+#define MGB_MV32(D, R) launch_mv32<D, R>(q, dev_sys_, rpt, grid, s)
+  MGB_CLASS_SWITCH(cls, MGB_MV32)
+#undef MGB_MV32
   count_launches(1);
   MGB_CUDA(cudaGetLastError());
   return MGB_OK;
@@ -1100,16 +1115,9 @@ int BatchEngine::enqueue_mv64(int cls, int mode, cudaStream_t s) {
   const WorkQueue q = make_queue(items_[kListAll][cls], counters_, cls, mode, kListAll);
   const int grid = 2 * c_->num_sms;
   const double* t = c_->exp_table;
-  switch (cls) {
-    case 0: launch_mv64<2, 1>(q, dev_sys_, t, grid, s); break;
-    case 1: launch_mv64<2, 2>(q, dev_sys_, t, grid, s); break;
-    case 2: launch_mv64<2, 4>(q, dev_sys_, t, grid, s); break;
-    case 3: launch_mv64<2, 8>(q, dev_sys_, t, grid, s); break;
-    case 4: launch_mv64<3, 1>(q, dev_sys_, t, grid, s); break;
-    case 5: launch_mv64<3, 2>(q, dev_sys_, t, grid, s); break;
-    case 6: launch_mv64<3, 4>(q, dev_sys_, t, grid, s); break;
-    default: launch_mv64<3, 8>(q, dev_sys_, t, grid, s); break;
-  }
+#define MGB_MV64(D, R) launch_mv64<D, R>(q, dev_sys_, t, grid, s)
+  MGB_CLASS_SWITCH(cls, MGB_MV64)
+#undef MGB_MV64
   count_launches(1);
   MGB_CUDA(cudaGetLastError());
   return MGB_OK;
@@ -1121,16 +1129,9 @@ int BatchEngine::enqueue_true(int cls, cudaStream_t s) {
   const int grid = 2 * c_->num_sms;
   const int* np = counters_ + kOffPending;
   const double* t = c_->exp_table;
-  switch (cls) {
-    case 0: k_btrue<2, 1><<<grid, kTile, 0, s>>>(pending_, np, dev_sys_, t); break;
-    case 1: k_btrue<2, 2><<<grid, kTile, 0, s>>>(pending_, np, dev_sys_, t); break;
-    case 2: k_btrue<2, 4><<<grid, kTile, 0, s>>>(pending_, np, dev_sys_, t); break;
-    case 3: k_btrue<2, 8><<<grid, kTile, 0, s>>>(pending_, np, dev_sys_, t); break;
-    case 4: k_btrue<3, 1><<<grid, kTile, 0, s>>>(pending_, np, dev_sys_, t); break;
-    case 5: k_btrue<3, 2><<<grid, kTile, 0, s>>>(pending_, np, dev_sys_, t); break;
-    case 6: k_btrue<3, 4><<<grid, kTile, 0, s>>>(pending_, np, dev_sys_, t); break;
-    default: k_btrue<3, 8><<<grid, kTile, 0, s>>>(pending_, np, dev_sys_, t); break;
-  }
+#define MGB_TRUE(D, R) k_btrue<D, R><<<grid, kTile, 0, s>>>(pending_, np, dev_sys_, t)
+  MGB_CLASS_SWITCH(cls, MGB_TRUE)
+#undef MGB_TRUE
   count_launches(1);
   MGB_CUDA(cudaGetLastError());
   return MGB_OK;
@@ -1244,10 +1245,10 @@ int BatchEngine::autotune() {
 // (Re)captures the step graph when the set of non-empty classes, the slot
 // range or a tuning choice changed.
 int BatchEngine::prepare_graph() {
-  unsigned int sig = 0;
-  for (int q = 0; q < kClasses; ++q) sig |= (has_mixed_[q] ? 1u : 0u) << q | (has_fp64_[q] ? 1u : 0u) << (q + 8);
-  sig = sig * 31u + (unsigned)nslots_;
-  for (int q = 0; q < kClasses; ++q) sig = sig * 31u + (unsigned)rpt_[q];
+  unsigned long long sig = 1469598103934665603ULL;  // FNV-1a over everything the capture bakes in
+  auto fold = [&](unsigned long long v) { sig = (sig ^ v) * 1099511628211ULL; };
+  for (int q = 0; q < kClasses; ++q) fold((has_mixed_[q] ? 1u : 0u) | (has_fp64_[q] ? 2u : 0u) | (unsigned)rpt_[q] << 2);
+  fold((unsigned long long)nslots_);
   if (graph_exec_ && sig == graph_sig_) return MGB_OK;
   if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
   if (graph_) cudaGraphDestroy(graph_);

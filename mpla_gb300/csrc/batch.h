@@ -23,7 +23,7 @@ struct BatchLane {
 };
 
 // One system, resident in device memory.  Vectors are n x R interleaved
-// (element (i, k) at i * R + k); R is nrhs padded to 1, 2, 4 or 8.
+// (element (i, k) at i * R + k); R is nrhs, or 6 for 5 and 8 for 7.
 struct BatchSys {
   int in_use;
   int n, dim, R, nrhs;
@@ -63,7 +63,7 @@ struct VecItem {
 
 class BatchEngine {
  public:
-  static constexpr int kClasses = 8;        // (dim 2|3) x (R 1|2|4|8)
+  static constexpr int kClasses = MGB_BATCH_CLASSES;  // (dim 2|3) x (R 1|2|3|4|6|8)
   static constexpr int kStepsPerGraph = 8;  // CG iterations per graph replay
   static constexpr int kBranches = 3 * kClasses;  // concurrent launches of the matvec phase
   // Matvec item lists per class: every item (FP64 matvecs), the items whose
@@ -73,6 +73,7 @@ class BatchEngine {
   // device counters: matvec queues (claim, finished) per class and mode,
   // item counts per list and class, the active-system count, vector-phase
   // queues (claim, finished) per phase and the vector item count
+  static_assert(kClasses == 12, "class layout");
   static constexpr int kOffMv = 0;
   static constexpr int kOffCount = 6 * kClasses;
   static constexpr int kOffActive = kOffCount + kLists * kClasses;
@@ -139,7 +140,7 @@ class BatchEngine {
   cudaEvent_t fork_ev_ = nullptr;
   cudaGraph_t graph_ = nullptr;
   cudaGraphExec_t graph_exec_ = nullptr;
-  unsigned int graph_sig_ = 0;
+  unsigned long long graph_sig_ = 0;
   long long graph_kernels_ = 0;
 };
 

@@ -150,3 +150,26 @@ def batch_system(spec: BatchSpec, k: int, seed: int = 0) -> GaussProblem:
     pts = np.stack([uniform(seed, 1000 + 16 * k + j, n) for j in range(d)])
     b = np.stack([normal(seed, 1_000_000 + 16 * k + j, n) for j in range(r)], axis=1)
     return GaussProblem(points=pts, ell=float(spec.ell[k]), nugget=1e-4, b=b)
+
+
+def serving_requests(rate: float, window: float, seed: int = 0, n_lo: int = 1024, n_hi: int = 32768):
+    """Requests of the serving workload: Poisson arrival times at `rate` per
+    second over [0, window), n log-uniform in [n_lo, n_hi], d in {2, 3},
+    l ~ U[0.03, 0.2], nugget 1e-4, 1-4 N(0,1) right-hand sides, precision
+    alternating FP64 (0) / mixed (1).  Returns (arrival, id, scaled points
+    dim x n, b n x r, precision) tuples."""
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > window:
+            break
+        k = len(out)
+        n = int(np.exp(rng.uniform(np.log(n_lo), np.log(n_hi))))
+        dim = 2 + int(rng.random() < 0.5)
+        ell = float(rng.uniform(0.03, 0.2))
+        r = int(rng.integers(1, 5))
+        pts = np.stack([uniform(seed, 5000 + 16 * k + j, n) for j in range(dim)]) / (math.sqrt(2.0) * ell)
+        b = np.stack([normal(seed, 6_000_000 + 16 * k + j, n) for j in range(r)], axis=1)
+        out.append((t, k, pts, b, k % 2))
+    return out

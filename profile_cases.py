@@ -13,6 +13,7 @@ that ends by itself (a few hundred MB on the device at most):
   python profile_cases.py mixed_c3    # full mixed solve, n = 131072, d = 3, l = 0.08
   python profile_cases.py batch_trace # all 512 batch systems to 1e-10, per-replay times
   python profile_cases.py batch512    # 16 timed steps of all 512 batch systems
+  python profile_cases.py serving_sweep  # the serving configuration, 3 rates x ~32 requests
   python profile_cases.py all
 
 Prints the CUDA-event time per launch of each case.
@@ -198,6 +199,44 @@ def case_batch_trace(count=512, out="gpurun_out/batch_trace.csv"):
     batch.close()
 
 
+def case_serving_sweep(rates=(0.1, 0.2, 0.4), per_rate=32, out="gpurun_out/serving_sweep.json"):
+    """The serving configuration as specified: per arrival rate, Poisson
+    arrivals of about `per_rate` requests, n log-uniform in [1024, 32768],
+    d in {2,3}, l ~ U[0.03, 0.2], 1-4 N(0,1) right-hand sides, half FP64,
+    relres 1e-10, drained until every request has finished; p50/p99 latency
+    and solves/s per rate and per precision (JSON)."""
+    import json
+    import time
+
+    from mpla_gb300.serve import Request, Server, latency_stats
+
+    res = []
+    for q, rate in enumerate(rates):
+        window = per_rate / rate
+        reqs = synth.serving_requests(rate, window, seed=100 + q)
+        batch = mg.Batch(256)
+        srv = Server(batch, slice_steps=64)
+        t0 = time.perf_counter()
+        for a, k, pts, b, prec in reqs:
+            srv.submit(Request(arrival=t0 + a, rid=k, points=pts, b=b, precision=prec))
+        srv.serve(until=t0 + window)
+        st = latency_stats(srv.done)
+        for p, name in ((0, "fp64"), (1, "mixed")):
+            lat = [c.latency for c in srv.done if c.precision == p]
+            if lat:
+                st[name] = {"completed": len(lat), "p50_s": float(np.percentile(lat, 50)),
+                            "p99_s": float(np.percentile(lat, 99)), "n_max": max(c.n for c in srv.done if c.precision == p)}
+        st.update({"rate_per_s": rate, "window_s": window, "submitted": len(reqs),
+                   "unfinished": len(reqs) - len(srv.done),
+                   "all_converged": all(int(i.status) == 0 for c in srv.done for i in c.infos),
+                   "wall_s": time.perf_counter() - t0})
+        batch.close()
+        print(json.dumps(st), flush=True)
+        res.append(st)
+    Path(out).parent.mkdir(parents=True, exist_ok=True)
+    Path(out).write_text(json.dumps(res, indent=1))
+
+
 def case_mixed_c3():
     """The mixed-precision configuration: n = 131072 points U[0,1]^3, l = 0.08,
     nugget 1e-4, b = sin(2 pi x1) cos(2 pi x2), solved to relres 1e-10."""
@@ -223,12 +262,12 @@ def case_mixed_c3():
 CASES = {"dgemv": case_dgemv, "gauss_f64": case_gauss_f64, "gauss_mixed": case_gauss_mixed,
          "mixed_cg": case_mixed_cg, "batch": case_batch, "batch128": case_batch128,
          "batch128_solve": case_batch128_solve, "mixed_c3": case_mixed_c3, "batch_trace": case_batch_trace,
-         "batch512": case_batch512}
+         "batch512": case_batch512, "serving_sweep": case_serving_sweep}
 
 
 def main(argv):
     mg.init(0)
-    long_cases = ("mixed_c3", "batch128", "batch128_solve", "batch_trace", "batch512")
+    long_cases = ("mixed_c3", "batch128", "batch128_solve", "batch_trace", "batch512", "serving_sweep")
     names = [k for k in CASES if k not in long_cases] if (not argv or argv[0] == "all") else argv
     for name in names:
         CASES[name]()

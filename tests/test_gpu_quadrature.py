@@ -13,7 +13,9 @@ quantity: the oracle needs 665 iterations, and 655 to 889 after relative
 perturbations of K by 1.1e-16 (a CPU measurement with the oracle), so the
 counts are compared within that spread (a factor 1.5).  The parity checks
 are on the results: the weights reach the tolerance on the FP64 oracle
-operator and integrate test functions like the oracle's weights.
+operator and integrate test functions as accurately as the oracle's weights
+(both within 5e-4 of the exact integrals; the oracle's weights miss them by
+up to 2.3e-4 after last-bit perturbations of K).
 """
 import os
 import re
@@ -71,13 +73,15 @@ def test_quadrature_weights_match_oracle_with_checkpoint_restart(app, orc, tmp_p
     assert st_orc == 0
     assert k_orc / 1.5 <= k <= 1.5 * k_orc, (k, k_orc)
     assert orc.true_relres(op, b, w) < 2 * tol
-    # weights integrate over [0,1]^3: 1 and x1 x2 x3 (1/8) like the oracle's
-    for f in (np.ones(n), pts[0] * pts[1] * pts[2]):
-        assert abs(f @ w - f @ w_orc) < 1e-5
+    # the weights integrate over [0,1]^3 like the oracle's: 1, x1 x2 x3 and
+    # exp(-x1) within 5e-4 of the exact integrals (the oracle's own weights
+    # miss them by up to 2.3e-4 after 1.1e-16 perturbations of K)
+    for f, exact in ((np.ones(n), 1.0), (pts[0] * pts[1] * pts[2], 0.125), (np.exp(-pts[0]), 1.0 - np.exp(-1.0))):
+        assert abs(f @ w - exact) < 5e-4 and abs(f @ w_orc - exact) < 5e-4
 
     # restart from the checkpoint files of the first run (x, r, d, z)
     k2, _ = run(app, tmp_path, n, dim, tol, 1, 200)
     st, w2 = orc.load_vector(str(tmp_path / "weights.dat"), n)
     assert st == 0
     assert orc.true_relres(op, b, w2) < 2 * tol
-    assert abs(np.sum(w2) - np.sum(w)) < 1e-5
+    assert abs(np.sum(w2) - 1.0) < 5e-4
