@@ -7,8 +7,13 @@
 //     (VEC = 2) coalesced, L1-bypassing loads, 8 columns in flight per thread;
 //   * the CTA's slice of x is staged in shared memory by one bulk (TMA) copy;
 //   * warp partials are summed in shared memory in warp order, and chunk
-//     partials across the grid by the last-arriving CTA of each strip in
-//     chunk order — a fixed summation order, so results are bit-reproducible.
+//     partials in chunk order: when a strip's chunks fit in one thread-block
+//     cluster (at most 8), CTA 0 of the cluster reads the others' partials
+//     from their shared memory (no global partials, fences or atomics);
+//     otherwise the last-arriving CTA of each strip reads them from global
+//     memory.  A fixed summation order either way, so results are
+//     bit-reproducible and the same on both paths.
+#include <cooperative_groups.h>
 #include <mutex>
 
 #include "internal.h"
@@ -20,6 +25,7 @@ namespace {
 
 constexpr int kWarps = 8;
 constexpr int kThreads = kWarps * 32;
+constexpr int kMaxCluster = 8;  // portable thread-block cluster size
 
 __device__ __forceinline__ double2 ld_stream2(const double* p) {
   double2 v;
@@ -35,7 +41,9 @@ __device__ __forceinline__ double ld_stream1(const double* p) {
 
 // BULK: stage x with one bulk copy and a bounded mbarrier wait (a wait that
 // gives up sets DEV_ERR_WAIT_TIMEOUT in *err); otherwise with plain loads.
-template <int VEC, bool BULK>
+// CLUSTER: the nsplit chunks of a strip form one cluster (rank = chunk) and
+// are reduced through distributed shared memory.
+template <int VEC, bool BULK, bool CLUSTER>
 __global__ void __launch_bounds__(kThreads) dgemv_kernel(int m, int n, const double* __restrict__ A,
                                                          long long lda, const double* __restrict__ x,
                                                          double* __restrict__ y, int cpw, int nsplit,
@@ -135,6 +143,19 @@ __global__ void __launch_bounds__(kThreads) dgemv_kernel(int m, int n, const dou
     if (lr < kRows && row0 + lr < m) y[row0 + lr] = cta_sum;
     return;
   }
+  if (CLUSTER) {
+    __shared__ double cpart[kRows];
+    if (lr < kRows) cpart[lr] = cta_sum;
+    cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
+    cl.sync();  // every chunk's partials are in its shared memory
+    if (split == 0 && lr < kRows && row0 + lr < m) {
+      double s = 0.0;
+      for (int q = 0; q < nsplit; ++q) s += *cl.map_shared_rank(&cpart[lr], q);
+      y[row0 + lr] = s;
+    }
+    cl.sync();  // keep every CTA's shared memory until CTA 0 has read it
+    return;
+  }
   if (lr < kRows && row0 + lr < m) partials[(long long)split * m + row0 + lr] = cta_sum;
   if (last_block_arrival(&tickets[strip], nsplit, &s_last)) {
     if (lr < kRows && row0 + lr < m) {
@@ -176,22 +197,53 @@ int launch_dgemv(DeviceContext* c, int m, int n, const double* A, int lda, const
   int cpw = 128;
   const long long target = 6LL * c->num_sms;
   while (cpw > 16 && (long long)strips * ((n + kWarps * cpw - 1) / (kWarps * cpw)) < target) cpw >>= 1;
-  const int nsplit = (n + kWarps * cpw - 1) / (kWarps * cpw);
-  if (nsplit > 1) {
+  int nsplit = (n + kWarps * cpw - 1) / (kWarps * cpw);
+  // Cluster reduction when a strip's chunks fit in a portable cluster (8),
+  // widening the chunks if that still leaves >= 2 CTAs per SM.
+  int ccpw = cpw;
+  while (ccpw < 512 && (n + kWarps * ccpw - 1) / (kWarps * ccpw) > kMaxCluster) ccpw <<= 1;
+  const int csplit = (n + kWarps * ccpw - 1) / (kWarps * ccpw);
+  const bool cluster = csplit > 1 && csplit <= kMaxCluster && (long long)strips * csplit >= 2LL * c->num_sms;
+  if (cluster) {
+    cpw = ccpw;
+    nsplit = csplit;
+  } else if (nsplit > 1) {
     MGB_TRY(ensure_split_partials(c, (size_t)nsplit * m));
     MGB_TRY(ensure_tickets(c, strips + 1));
   }
   const size_t smem = 16 + sizeof(double) * (kWarps * cpw + kWarps * rows_per_strip);
   const long long grid = (long long)strips * nsplit;
   if (grid > 0x7fffffffLL) return set_error(MGB_ERR_ARG, "dgemv: grid too large");
-  if (vec2) {
-    dgemv_kernel<2, true><<<(unsigned)grid, kThreads, smem, s>>>(m, n, A, lda, x, y, cpw, nsplit,
-                                                               c->split_partials, c->tickets + 1, done,
-                                                               c->dev_error);
+  if (cluster) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)nsplit;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    long long lda_ll = lda;
+    double* no_partials = nullptr;
+    unsigned int* no_tickets = nullptr;
+    if (vec2)
+      MGB_CUDA(cudaLaunchKernelEx(&cfg, dgemv_kernel<2, true, true>, m, n, A, lda_ll, x, y, cpw, nsplit, no_partials,
+                                  no_tickets, done, c->dev_error));
+    else
+      MGB_CUDA(cudaLaunchKernelEx(&cfg, dgemv_kernel<1, true, true>, m, n, A, lda_ll, x, y, cpw, nsplit, no_partials,
+                                  no_tickets, done, c->dev_error));
+  } else if (vec2) {
+    dgemv_kernel<2, true, false><<<(unsigned)grid, kThreads, smem, s>>>(m, n, A, lda, x, y, cpw, nsplit,
+                                                                      c->split_partials, c->tickets + 1, done,
+                                                                      c->dev_error);
   } else {
-    dgemv_kernel<1, true><<<(unsigned)grid, kThreads, smem, s>>>(m, n, A, lda, x, y, cpw, nsplit,
-                                                               c->split_partials, c->tickets + 1, done,
-                                                               c->dev_error);
+    dgemv_kernel<1, true, false><<<(unsigned)grid, kThreads, smem, s>>>(m, n, A, lda, x, y, cpw, nsplit,
+                                                                      c->split_partials, c->tickets + 1, done,
+                                                                      c->dev_error);
   }
   count_launches(1);
   MGB_CUDA(cudaGetLastError());
@@ -281,10 +333,10 @@ extern "C" int mgb_dgemv_noalloc(int m, int n, const double* A, int lda, const d
   // x is staged with plain loads: this variant has no device-side wait, so
   // no error word exists that a caller would have to read back.
   if (vec2) {
-    dgemv_kernel<2, false><<<(unsigned)grid, kThreads, smem, s>>>(m, n, A, lda, x, y, cpw, nsplit, partials,
+    dgemv_kernel<2, false, false><<<(unsigned)grid, kThreads, smem, s>>>(m, n, A, lda, x, y, cpw, nsplit, partials,
                                                                 tickets + 1, nullptr, nullptr);
   } else {
-    dgemv_kernel<1, false><<<(unsigned)grid, kThreads, smem, s>>>(m, n, A, lda, x, y, cpw, nsplit, partials,
+    dgemv_kernel<1, false, false><<<(unsigned)grid, kThreads, smem, s>>>(m, n, A, lda, x, y, cpw, nsplit, partials,
                                                                 tickets + 1, nullptr, nullptr);
   }
   count_launches(1);
