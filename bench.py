@@ -333,8 +333,8 @@ def bench_serving(mg, rates, per_rate: int, n_hi: int, drain: float, seed: int =
     for q, rate in enumerate(rates):
         window = per_rate / rate
         reqs = synth.serving_requests(rate, window, seed=seed + q, n_hi=n_hi)
-        batch = mg.Batch(256)
-        srv = Server(batch, slice_steps=64)
+        engines = {mg.PREC_FP64: mg.Batch(128), mg.PREC_MIXED: mg.Batch(128)}
+        srv = Server(engines, slice_steps=64)
         t0 = time.perf_counter()
         for a, k, pts, b, prec in reqs:
             srv.submit(Request(arrival=t0 + a, rid=k, points=pts, b=b, precision=prec))
@@ -348,7 +348,8 @@ def bench_serving(mg, rates, per_rate: int, n_hi: int, drain: float, seed: int =
                 by_prec[name] = {"completed": len(lat), "p50_s": float(np.percentile(lat, 50)),
                                  "p99_s": float(np.percentile(lat, 99)),
                                  "n_max": int(max(c.n for c in srv.done if c.precision == p))}
-        batch.close()
+        for e in engines.values():
+            e.close()
         st.update({"rate_per_s": rate, "window_s": window,
                    "workload": f"Poisson arrivals {rate}/s for {window:g} s, n log-uniform [1024,{n_hi}], "
                                "d in {2,3}, l ~ U[0.03,0.2], 1-4 N(0,1) right-hand sides, half FP64 / half mixed, "

@@ -207,6 +207,14 @@ int mgb_batch_add(mgb_batch* b, int n, int dim, const double* coords_host, doubl
 /* Advance every admitted system by up to max_steps iterations (whole
  * graph replays); *active = systems with a right-hand side still running. */
 int mgb_batch_run(mgb_batch* b, int max_steps, int* active);
+/* The same in two halves, so that several batches run at once: run_async
+ * enqueues up to max_steps iterations on the batch's own stream (every batch
+ * has one) and returns; wait synchronises with it, retires finished systems
+ * from the work lists and sets *active.  A serving loop keeps FP64 and mixed
+ * requests in separate batches and overlaps their steps this way (FP64 work
+ * uses the FP64 pipe, mixed work the FP32 and SFU pipes). */
+int mgb_batch_run_async(mgb_batch* b, int max_steps);
+int mgb_batch_wait(mgb_batch* b, int* active);
 /* Handles of systems whose right-hand sides have all finished. */
 int mgb_batch_finished(mgb_batch* b, int* handles, int capacity, int* count);
 /* Copy x (column-major, n x nrhs) and one mgb_solve_info per right-hand side

@@ -46,7 +46,8 @@ C_ABI_SYMBOLS = (
     "mgb_cg_dense", "mgb_bicgstab_dense", "mgb_cg_gauss", "mgb_bicgstab_gauss", "mgb_cg_gauss_host",
     "mgb_kernel_launches", "mgb_time_gauss_matvec", "mgb_time_dgemv",
     "mgb_save_vector", "mgb_load_vector",
-    "mgb_batch_create", "mgb_batch_add", "mgb_batch_run", "mgb_batch_finished", "mgb_batch_result",
+    "mgb_batch_create", "mgb_batch_add", "mgb_batch_run", "mgb_batch_run_async", "mgb_batch_wait",
+    "mgb_batch_finished", "mgb_batch_result",
     "mgb_batch_tuning", "mgb_batch_destroy",
     "mgb_set_mixed_matvec", "mgb_get_mixed_matvec", "mgb_gauss_mixed_work",
     "mgb_register_generic_device_code", "mgb_unregister_generic_device_code",
@@ -117,6 +118,8 @@ _SIGS = {
     "mgb_batch_create": (_I, [_I, C.POINTER(_P)]),
     "mgb_batch_add": (_I, [_P, _I, _I, _P, _D, _I, _P, _I, _D, _I, C.c_size_t, C.POINTER(_I)]),
     "mgb_batch_run": (_I, [_P, _I, C.POINTER(_I)]),
+    "mgb_batch_run_async": (_I, [_P, _I]),
+    "mgb_batch_wait": (_I, [_P, C.POINTER(_I)]),
     "mgb_batch_finished": (_I, [_P, _P, _I, C.POINTER(_I)]),
     "mgb_batch_result": (_I, [_P, _I, _P, C.POINTER(SolveInfo), _I]),
     "mgb_batch_tuning": (_I, [_P, _P, _P]),
@@ -393,6 +396,16 @@ class Batch:
         number of systems still running."""
         act = _I()
         check(lib().mgb_batch_run(self._h, int(min(max_steps, 2**31 - 1)), C.byref(act)))
+        return act.value
+
+    def run_async(self, max_steps: int) -> None:
+        """Enqueue up to ``max_steps`` iterations on the batch's own stream."""
+        check(lib().mgb_batch_run_async(self._h, int(min(max_steps, 2**31 - 1))))
+
+    def wait(self) -> int:
+        """Wait for the enqueued iterations; returns the systems still running."""
+        act = _I()
+        check(lib().mgb_batch_wait(self._h, C.byref(act)))
         return act.value
 
     def finished(self) -> list[int]:

@@ -794,6 +794,10 @@ constexpr int kWidths[6] = {1, 2, 3, 4, 6, 8};
 // --------------------------------------------------------------- engine
 int BatchEngine::init(DeviceContext* c, int max_systems, cudaStream_t s) {
   c_ = c;
+  if (!s) {
+    MGB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    own_stream_ = true;
+  }
   s_ = s;
   max_ = max_systems;
   host_.assign(max_systems, BatchSys{});
@@ -843,6 +847,7 @@ BatchEngine::~BatchEngine() {
     if (join_ev_[i]) cudaEventDestroy(join_ev_[i]);
   }
   if (fork_ev_) cudaEventDestroy(fork_ev_);
+  if (own_stream_) cudaStreamDestroy(s_);
 }
 
 int BatchEngine::class_of(int dim, int R) {
@@ -1289,6 +1294,32 @@ int BatchEngine::run_steps(int steps, int* active_out) {
   return MGB_OK;
 }
 
+int BatchEngine::run_async(int steps) {
+  MGB_TRY(sync_items());
+  MGB_TRY(autotune());
+  if (listed_count_ == 0 || steps <= 0) return MGB_OK;
+  for (int done_steps = 0; done_steps < steps; done_steps += kStepsPerGraph) {
+    MGB_TRY(prepare_graph());
+    MGB_CUDA(cudaGraphLaunch(graph_exec_, s_));
+    count_launches(graph_kernels_);
+  }
+  MGB_CUDA(cudaMemcpyAsync(active_host_, counters_ + kOffActive, sizeof(int), cudaMemcpyDeviceToHost, s_));
+  launched_ = true;
+  return MGB_OK;
+}
+
+int BatchEngine::wait(int* active_out) {
+  MGB_CUDA(cudaStreamSynchronize(s_));
+  const int active = launched_ ? *active_host_ : listed_count_;
+  launched_ = false;
+  if (active < listed_count_) {  // systems finished in these replays
+    MGB_TRY(prune_finished());
+    MGB_TRY(sync_items());
+  }
+  if (active_out) *active_out = active;
+  return MGB_OK;
+}
+
 int BatchEngine::result(int handle, double* x_host, mgb_solve_info* info, bool release) {
   if (handle < 0 || handle >= max_ || !host_[handle].in_use)
     return set_error(MGB_ERR_ARG, "bad batch handle %d", handle);
@@ -1354,7 +1385,7 @@ int mgb_batch_create(int max_systems, mgb_batch** out) {
   DeviceContext* c = nullptr;
   MGB_TRY(context(&c));
   mgb_batch* b = new mgb_batch();
-  const int st = b->engine.init(c, max_systems, c->stream);
+  const int st = b->engine.init(c, max_systems, nullptr);  // a stream of its own
   if (st != MGB_OK) {
     delete b;
     return st;
@@ -1372,6 +1403,16 @@ int mgb_batch_add(mgb_batch* b, int n, int dim, const double* coords_host, doubl
 int mgb_batch_run(mgb_batch* b, int max_steps, int* active) {
   if (!b) return set_error(MGB_ERR_ARG, "mgb_batch_run: null batch");
   return b->engine.run_steps(max_steps, active);
+}
+
+int mgb_batch_run_async(mgb_batch* b, int max_steps) {
+  if (!b) return set_error(MGB_ERR_ARG, "mgb_batch_run_async: null batch");
+  return b->engine.run_async(max_steps);
+}
+
+int mgb_batch_wait(mgb_batch* b, int* active) {
+  if (!b) return set_error(MGB_ERR_ARG, "mgb_batch_wait: null batch");
+  return b->engine.wait(active);
 }
 
 int mgb_batch_finished(mgb_batch* b, int* handles, int capacity, int* count) {

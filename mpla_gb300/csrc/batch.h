@@ -87,6 +87,11 @@ class BatchEngine {
   int add(int n, int dim, const double* coords_host, double nugget, int nrhs, const double* b_host,
           int precision, double eps, int iter_max, size_t reserve_bytes, int* handle);
   int run_steps(int steps, int* active_out);
+  // Enqueue up to `steps` iterations (whole graph replays) without waiting;
+  // wait() then synchronises, retires finished systems from the work lists
+  // and reports the systems still running.
+  int run_async(int steps);
+  int wait(int* active_out);
   int done_handles(std::vector<int>* out);
   int result(int handle, double* x_host, mgb_solve_info* info, bool release);
   const int* rows_per_thread() const { return rpt_; }
@@ -112,6 +117,8 @@ class BatchEngine {
 
   DeviceContext* c_ = nullptr;
   cudaStream_t s_ = nullptr;
+  bool own_stream_ = false;  // s_ created by init (destroyed with the engine)
+  bool launched_ = false;    // replays enqueued since the last wait()
   int max_ = 0;
   int nslots_ = 0;
   std::vector<BatchSys> host_;

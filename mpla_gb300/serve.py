@@ -3,10 +3,13 @@
 Requests (a Gaussian system with 1..8 right-hand sides and a precision)
 arrive over time.  The loop:
   1. admits every arrived request whose buffers fit in free device memory
-     (the engine refuses otherwise; the request waits in the queue),
-  2. advances all admitted systems by a slice of CG iterations (one or more
-     replays of the engine's step graph -- every system's work overlaps on
-     the device),
+     (the engine refuses otherwise; the request waits in the queue) into the
+     engine of its precision,
+  2. advances all admitted systems by a slice of CG iterations: each engine
+     enqueues its graph replays on its own stream, then the loop waits for
+     all of them, so FP64 and mixed work overlap on the device (FP64 on the
+     FP64 pipe, mixed on the FP32 and SFU pipes) and a mixed request's
+     steps never wait for the much slower FP64 steps,
   3. retires the systems whose right-hand sides have all finished, records
      their latency (arrival to result on the host), and frees their slots.
 So requests arriving while others are on the GPU join at the next slice, and
@@ -55,20 +58,31 @@ class Completion:
 
 
 class Server:
-    """Drives an engine with the Batch interface (add/run/finished/result)."""
+    """Drives engines with the Batch interface (add / run_async / wait /
+    finished / result): one engine for every precision, or one engine for
+    all (``engine`` may be a single engine or a dict precision -> engine)."""
 
     def __init__(self, engine, slice_steps: int = 64, reserve_bytes: int = 2 << 30, iter_max: int = 200000,
                  clock=time.perf_counter, sleep=time.sleep):
-        self.engine = engine
+        self.engines = engine if isinstance(engine, dict) else None
+        self.engine = None if self.engines else engine
         self.slice_steps = slice_steps
         self.reserve_bytes = reserve_bytes
         self.iter_max = iter_max
         self.clock = clock
         self.sleep = sleep
         self.queue: list[Request] = []       # submitted, not yet admitted (ordered by arrival)
-        self.running: dict[int, tuple] = {}  # handle -> (request, admitted time)
+        self.running: dict[tuple, tuple] = {}  # (engine key, handle) -> (request, admitted time)
         self.done: list[Completion] = []
         self.refusals = 0
+
+    def _engine_of(self, precision: int):
+        if self.engines is None:
+            return 0, self.engine
+        return precision, self.engines[precision]
+
+    def _all_engines(self):
+        return [(0, self.engine)] if self.engines is None else list(self.engines.items())
 
     def submit(self, req: Request) -> None:
         heapq.heappush(self.queue, req)
@@ -77,34 +91,38 @@ class Server:
         waiting = []
         while self.queue and self.queue[0].arrival <= now:
             req = heapq.heappop(self.queue)
+            key, eng = self._engine_of(req.precision)
             try:
-                h = self.engine.add(req.points, req.nugget, req.b, precision=req.precision, eps=req.eps,
-                                    iter_max=self.iter_max, reserve_bytes=self.reserve_bytes)
+                h = eng.add(req.points, req.nugget, req.b, precision=req.precision, eps=req.eps,
+                            iter_max=self.iter_max, reserve_bytes=self.reserve_bytes)
             except Exception as e:  # noqa: BLE001 - only a memory/slot refusal is retried
                 if getattr(e, "status", None) == NOMEM:
                     self.refusals += 1
                     waiting.append(req)
                     continue
                 raise
-            self.running[h] = (req, self.clock())
+            self.running[(key, h)] = (req, self.clock())
         for r in waiting:
             heapq.heappush(self.queue, r)
 
-    def _retire(self) -> None:
-        for h in self.engine.finished():
-            if h not in self.running:
+    def _retire(self, key, eng) -> None:
+        for h in eng.finished():
+            if (key, h) not in self.running:
                 continue
-            req, admitted = self.running.pop(h)
+            req, admitted = self.running.pop((key, h))
             n, r = req.b.shape[0], req.b.shape[1]
-            x, infos = self.engine.result(h, n, r, release=True)
+            x, infos = eng.result(h, n, r, release=True)
             self.done.append(Completion(req.rid, n, r, req.precision, req.arrival, admitted, self.clock(), x, infos))
 
     def step(self) -> int:
         """One scheduling round; returns the number of running systems."""
         self._admit(self.clock())
-        if self.running:
-            self.engine.run(max_steps=self.slice_steps)
-            self._retire()
+        busy = [(k, e) for k, e in self._all_engines() if any(key == k for key, _ in self.running)]
+        for _, eng in busy:
+            eng.run_async(self.slice_steps)
+        for key, eng in busy:
+            eng.wait()
+            self._retire(key, eng)
         return len(self.running)
 
     def serve(self, until: float, drain_until: float | None = None) -> None:

@@ -214,8 +214,8 @@ def case_serving_sweep(rates=(0.1, 0.2, 0.4), per_rate=32, out="gpurun_out/servi
     for q, rate in enumerate(rates):
         window = per_rate / rate
         reqs = synth.serving_requests(rate, window, seed=100 + q)
-        batch = mg.Batch(256)
-        srv = Server(batch, slice_steps=64)
+        engines = {mg.PREC_FP64: mg.Batch(128), mg.PREC_MIXED: mg.Batch(128)}
+        srv = Server(engines, slice_steps=64)
         t0 = time.perf_counter()
         for a, k, pts, b, prec in reqs:
             srv.submit(Request(arrival=t0 + a, rid=k, points=pts, b=b, precision=prec))
@@ -230,7 +230,8 @@ def case_serving_sweep(rates=(0.1, 0.2, 0.4), per_rate=32, out="gpurun_out/servi
                    "unfinished": len(reqs) - len(srv.done),
                    "all_converged": all(int(i.status) == 0 for c in srv.done for i in c.infos),
                    "wall_s": time.perf_counter() - t0})
-        batch.close()
+        for e in engines.values():
+            e.close()
         print(json.dumps(st), flush=True)
         res.append(st)
     Path(out).parent.mkdir(parents=True, exist_ok=True)

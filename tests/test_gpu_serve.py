@@ -36,8 +36,8 @@ def test_served_results_are_correct_and_match_solo_solves(gpu, orc):
     # one mixed and one FP64 request of the serving configuration's larger
     # sizes, arriving while the others run
     reqs += [make_request(len(reqs) + j, t0 + 0.5, rng, n=8192 + 96 * j) for j in range(2)]
-    batch = gpu.Batch(64)
-    srv = Server(batch, slice_steps=32)
+    engines = {gpu.PREC_FP64: gpu.Batch(64), gpu.PREC_MIXED: gpu.Batch(64)}
+    srv = Server(engines, slice_steps=32)
     for r in reqs:
         srv.submit(r)
     srv.serve(until=t0 + 1.0, drain_until=t0 + 300.0)
@@ -60,4 +60,5 @@ def test_served_results_are_correct_and_match_solo_solves(gpu, orc):
         x, _ = solo.result(h, req.b.shape[0], req.b.shape[1])
         solo.close()
         assert np.array_equal(x, by_id[req.rid].x)
-    batch.close()
+    for e in engines.values():
+        e.close()

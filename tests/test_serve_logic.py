@@ -61,6 +61,13 @@ class FakeEngine:
             self.left[h] -= 1
         return sum(1 for v in self.left.values() if v > 0)
 
+    def run_async(self, max_steps):
+        self.pending = max_steps
+
+    def wait(self):
+        self.waits = getattr(self, "waits", 0) + 1
+        return self.run(self.pending)
+
     def finished(self):
         return [h for h, v in self.left.items() if v <= 0]
 
@@ -112,3 +119,20 @@ def test_poisson_arrivals_rate():
     a = poisson_arrivals(50.0, 100.0, rng)
     assert abs(len(a) / 100.0 - 50.0) < 3.0
     assert all(x < y for x, y in zip(a, a[1:]))
+
+
+def test_server_keeps_precisions_in_their_own_engines():
+    """FP64 and mixed requests go to separate engines, both of which advance
+    in every round (their device work overlaps); each engine's handles are
+    its own."""
+    clock = FakeClock()
+    engines = {0: FakeEngine(clock, budget=10**9), 1: FakeEngine(clock, budget=10**9)}
+    srv = Server(engines, clock=clock, sleep=clock.sleep)
+    for k in range(6):
+        n = 300 + 100 * k
+        srv.submit(Request(arrival=0.01 * k, rid=k, points=np.zeros((2, n)), b=np.zeros((n, 1)), precision=k % 2))
+    srv.serve(until=0.1, drain_until=100.0)
+    assert sorted(c.rid for c in srv.done) == list(range(6))
+    assert all(e.used == 0 and e.next == 3 for e in engines.values())
+    assert all(c.precision == c.rid % 2 for c in srv.done)
+    assert engines[0].waits > 1 and engines[1].waits > 1
