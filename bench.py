@@ -641,7 +641,7 @@ def main(argv=None):
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--n", type=int, default=N_FULL)
     p.add_argument("--iter-max", type=int, default=100000)
-    p.add_argument("--e2e-steps", type=int, default=1)
+    p.add_argument("--e2e-steps", type=int, default=3)
     p.add_argument("--fp64-sample-iters", type=int, default=20)
     p.add_argument("--fp64-iterations", type=int, default=0,
                    help="FP64 CG iteration count of the full solve, when known (used to scale sampled iterations)")

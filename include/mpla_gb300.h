@@ -212,9 +212,13 @@ int mgb_batch_run(mgb_batch* b, int max_steps, int* active);
  * has one) and returns; wait synchronises with it, retires finished systems
  * from the work lists and sets *active.  A serving loop keeps FP64 and mixed
  * requests in separate batches and overlaps their steps this way (FP64 work
- * uses the FP64 pipe, mixed work the FP32 and SFU pipes). */
+ * uses the FP64 pipe, mixed work the FP32 and SFU pipes), each batch
+ * starting its next slice as soon as its last one has finished. */
 int mgb_batch_run_async(mgb_batch* b, int max_steps);
 int mgb_batch_wait(mgb_batch* b, int* active);
+/* *ready = 1 when the iterations enqueued by run_async have finished (so
+ * that mgb_batch_wait returns without blocking), else 0. */
+int mgb_batch_ready(mgb_batch* b, int* ready);
 /* Handles of systems whose right-hand sides have all finished. */
 int mgb_batch_finished(mgb_batch* b, int* handles, int capacity, int* count);
 /* Copy x (column-major, n x nrhs) and one mgb_solve_info per right-hand side

@@ -46,7 +46,7 @@ C_ABI_SYMBOLS = (
     "mgb_cg_dense", "mgb_bicgstab_dense", "mgb_cg_gauss", "mgb_bicgstab_gauss", "mgb_cg_gauss_host",
     "mgb_kernel_launches", "mgb_time_gauss_matvec", "mgb_time_dgemv",
     "mgb_save_vector", "mgb_load_vector",
-    "mgb_batch_create", "mgb_batch_add", "mgb_batch_run", "mgb_batch_run_async", "mgb_batch_wait",
+    "mgb_batch_create", "mgb_batch_add", "mgb_batch_run", "mgb_batch_run_async", "mgb_batch_wait", "mgb_batch_ready",
     "mgb_batch_finished", "mgb_batch_result",
     "mgb_batch_tuning", "mgb_batch_destroy",
     "mgb_set_mixed_matvec", "mgb_get_mixed_matvec", "mgb_gauss_mixed_work",
@@ -120,6 +120,7 @@ _SIGS = {
     "mgb_batch_run": (_I, [_P, _I, C.POINTER(_I)]),
     "mgb_batch_run_async": (_I, [_P, _I]),
     "mgb_batch_wait": (_I, [_P, C.POINTER(_I)]),
+    "mgb_batch_ready": (_I, [_P, C.POINTER(_I)]),
     "mgb_batch_finished": (_I, [_P, _P, _I, C.POINTER(_I)]),
     "mgb_batch_result": (_I, [_P, _I, _P, C.POINTER(SolveInfo), _I]),
     "mgb_batch_tuning": (_I, [_P, _P, _P]),
@@ -407,6 +408,12 @@ class Batch:
         act = _I()
         check(lib().mgb_batch_wait(self._h, C.byref(act)))
         return act.value
+
+    def ready(self) -> bool:
+        """True when the iterations enqueued by run_async have finished."""
+        r = _I()
+        check(lib().mgb_batch_ready(self._h, C.byref(r)))
+        return bool(r.value)
 
     def finished(self) -> list[int]:
         buf = (_I * self.max_systems)()

@@ -1320,6 +1320,17 @@ int BatchEngine::wait(int* active_out) {
   return MGB_OK;
 }
 
+int BatchEngine::ready(int* ready_out) {
+  const cudaError_t e = cudaStreamQuery(s_);
+  if (e == cudaErrorNotReady) {
+    *ready_out = 0;
+    return MGB_OK;
+  }
+  MGB_CUDA(e);
+  *ready_out = 1;
+  return MGB_OK;
+}
+
 int BatchEngine::result(int handle, double* x_host, mgb_solve_info* info, bool release) {
   if (handle < 0 || handle >= max_ || !host_[handle].in_use)
     return set_error(MGB_ERR_ARG, "bad batch handle %d", handle);
@@ -1413,6 +1424,11 @@ int mgb_batch_run_async(mgb_batch* b, int max_steps) {
 int mgb_batch_wait(mgb_batch* b, int* active) {
   if (!b) return set_error(MGB_ERR_ARG, "mgb_batch_wait: null batch");
   return b->engine.wait(active);
+}
+
+int mgb_batch_ready(mgb_batch* b, int* ready) {
+  if (!b || !ready) return set_error(MGB_ERR_ARG, "mgb_batch_ready: null argument");
+  return b->engine.ready(ready);
 }
 
 int mgb_batch_finished(mgb_batch* b, int* handles, int capacity, int* count) {

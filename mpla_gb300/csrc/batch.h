@@ -92,6 +92,8 @@ class BatchEngine {
   // and reports the systems still running.
   int run_async(int steps);
   int wait(int* active_out);
+  // 1 when the enqueued iterations have finished (wait() then does not block)
+  int ready(int* ready_out);
   int done_handles(std::vector<int>* out);
   int result(int handle, double* x_host, mgb_solve_info* info, bool release);
   const int* rows_per_thread() const { return rpt_; }

@@ -44,7 +44,7 @@ __device__ __forceinline__ double ld_stream1(const double* p) {
 // CLUSTER: the nsplit chunks of a strip form one cluster (rank = chunk) and
 // are reduced through distributed shared memory.
 template <int VEC, bool BULK, bool CLUSTER>
-__global__ void __launch_bounds__(kThreads, 4) dgemv_kernel(int m, int n, const double* __restrict__ A,
+__global__ void __launch_bounds__(kThreads) dgemv_kernel(int m, int n, const double* __restrict__ A,
                                                          long long lda, const double* __restrict__ x,
                                                          double* __restrict__ y, int cpw, int nsplit,
                                                          double* __restrict__ partials,
@@ -96,44 +96,17 @@ __global__ void __launch_bounds__(kThreads, 4) dgemv_kernel(int m, int n, const 
     const double* a = A + (long long)(col0 + wc0) * lda + r;
     const bool pair = (VEC == 2) && (r + 1 < m);
     int j = wc0;
-    if (VEC == 2 && pair) {
-      // two register buffers of 4 columns: the next group's loads are in
-      // flight while this group's FMAs run (same column order, same sums;
-      // 4 CTAs of 256 threads stay resident per SM)
-      constexpr int G = 4;
-      const int jend = wc0 + ((wc1 - wc0) / G) * G;
-      double2 va[G], vb[G];
-      auto loadg = [&](double2(&v)[G], const double* p) {
+    for (; j + 8 <= wc1; j += 8) {
+      if (VEC == 2 && pair) {
+        double2 v[8];
 #pragma unroll
-        for (int u = 0; u < G; ++u) v[u] = ld_stream2(p + (long long)u * lda);
-      };
-      auto fmag = [&](const double2(&v)[G], int j0) {
+        for (int u = 0; u < 8; ++u) v[u] = ld_stream2(a + (long long)u * lda);
 #pragma unroll
-        for (int u = 0; u < G; ++u) {
-          const double xv = xs[j0 + u];
+        for (int u = 0; u < 8; ++u) {
+          const double xv = xs[j + u];
           acc0 = fma(v[u].x, xv, acc0);
           acc1 = fma(v[u].y, xv, acc1);
         }
-      };
-      if (j < jend) loadg(va, a);
-      while (j < jend) {
-        const bool more = j + G < jend;
-        if (more) loadg(vb, a + G * lda);
-        fmag(va, j);
-        a += G * lda;
-        j += G;
-        if (!more) break;
-        const bool more2 = j + G < jend;
-        if (more2) loadg(va, a + G * lda);
-        fmag(vb, j);
-        a += G * lda;
-        j += G;
-        if (!more2) break;
-      }
-    }
-    for (; j + 8 <= wc1; j += 8) {
-      if (VEC == 2 && pair) {
-        break;  // (handled above)
       } else {
         double v[8];
 #pragma unroll

@@ -75,6 +75,7 @@ class Server:
         self.running: dict[tuple, tuple] = {}  # (engine key, handle) -> (request, admitted time)
         self.done: list[Completion] = []
         self.refusals = 0
+        self.inflight: set = set()           # engines with a slice enqueued
 
     def _engine_of(self, precision: int):
         if self.engines is None:
@@ -115,15 +116,37 @@ class Server:
             self.done.append(Completion(req.rid, n, r, req.precision, req.arrival, admitted, self.clock(), x, infos))
 
     def step(self) -> int:
-        """One scheduling round; returns the number of running systems."""
+        """One scheduling round; returns the number of running systems.
+        Every engine with running systems works on its own slice: an engine
+        whose last slice has finished is retired and given the next one at
+        once, while the others keep running (so a fast engine never waits
+        for a slow one)."""
         self._admit(self.clock())
-        busy = [(k, e) for k, e in self._all_engines() if any(key == k for key, _ in self.running)]
-        for _, eng in busy:
-            eng.run_async(self.slice_steps)
-        for key, eng in busy:
-            eng.wait()
-            self._retire(key, eng)
+        started = False
+        for key, eng in self._all_engines():
+            busy = any(k == key for k, _ in self.running)
+            if key in self.inflight:
+                if not eng.ready():
+                    continue
+                self.inflight.discard(key)
+                eng.wait()
+                self._retire(key, eng)
+                busy = any(k == key for k, _ in self.running)
+            if busy:
+                eng.run_async(self.slice_steps)
+                self.inflight.add(key)
+                started = True
+        if not started and self.inflight:
+            self.sleep(0.0002)
         return len(self.running)
+
+    def drain(self) -> None:
+        """Wait for every slice in flight (their systems stay admitted)."""
+        for key, eng in self._all_engines():
+            if key in self.inflight:
+                eng.wait()
+                self._retire(key, eng)
+        self.inflight.clear()
 
     def serve(self, until: float, drain_until: float | None = None) -> None:
         """Run rounds until every submitted request has finished, or the clock
@@ -134,6 +157,7 @@ class Server:
         while True:
             now = self.clock()
             if now > drain_until:
+                self.drain()
                 break
             if not self.running and not self.queue:
                 if now >= until:

@@ -68,6 +68,9 @@ class FakeEngine:
         self.waits = getattr(self, "waits", 0) + 1
         return self.run(self.pending)
 
+    def ready(self):
+        return True
+
     def finished(self):
         return [h for h, v in self.left.items() if v <= 0]
 
@@ -136,3 +139,30 @@ def test_server_keeps_precisions_in_their_own_engines():
     assert all(e.used == 0 and e.next == 3 for e in engines.values())
     assert all(c.precision == c.rid % 2 for c in srv.done)
     assert engines[0].waits > 1 and engines[1].waits > 1
+
+
+class SlowEngine(FakeEngine):
+    """Finishes a slice only every `period`-th time it is asked."""
+
+    def __init__(self, clock, budget, period):
+        super().__init__(clock, budget)
+        self.period = period
+        self.asked = 0
+
+    def ready(self):
+        self.asked += 1
+        return self.asked % self.period == 0
+
+
+def test_fast_engine_does_not_wait_for_slow_engine():
+    clock = FakeClock()
+    engines = {0: SlowEngine(clock, 10**9, period=50), 1: FakeEngine(clock, 10**9)}
+    srv = Server(engines, clock=clock, sleep=clock.sleep)
+    srv.submit(Request(arrival=0.0, rid=0, points=np.zeros((2, 5000)), b=np.zeros((5000, 1)), precision=0))
+    srv.submit(Request(arrival=0.0, rid=1, points=np.zeros((2, 300)), b=np.zeros((300, 1)), precision=1))
+    srv.serve(until=0.0, drain_until=1000.0)
+    fin = {c.rid: c.finished for c in srv.done}
+    assert fin[1] < fin[0]
+    # the small request needed 3 slices of its engine and finished while the
+    # slow engine had completed only a few of its 50
+    assert engines[1].waits == 3
