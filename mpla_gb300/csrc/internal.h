@@ -79,6 +79,8 @@ struct DeviceContext {
   int n_tickets = 0;
   unsigned int* dev_error = nullptr;   // device error word
   SolverState* state_host = nullptr;   // pinned mirror of one SolverState
+  SolverState* state_ahead = nullptr;  // pinned mirrors of the solver loop's two chunks in flight
+  cudaEvent_t state_ev[2] = {nullptr, nullptr};
   std::map<size_t, std::vector<void*>> free_blocks;   // caching pool: size -> blocks
   std::map<void*, size_t> live_blocks;
   // split-K partials for dgemv / matvecs (grown on demand, never shrunk)

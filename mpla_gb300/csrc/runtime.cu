@@ -75,6 +75,8 @@ static int create_context(int dev, DeviceContext** out) {
   MGB_CUDA(cudaMalloc(&c->dev_error, sizeof(unsigned int)));
   MGB_CUDA(cudaMemset(c->dev_error, 0, sizeof(unsigned int)));
   MGB_CUDA(cudaMallocHost(&c->state_host, sizeof(SolverState)));
+  MGB_CUDA(cudaMallocHost(&c->state_ahead, 2 * sizeof(SolverState)));
+  for (int i = 0; i < 2; ++i) MGB_CUDA(cudaEventCreateWithFlags(&c->state_ev[i], cudaEventDisableTiming));
   MGB_TRY(ensure_tickets(c, 4096));
   *out = c;
   return MGB_OK;
@@ -171,6 +173,9 @@ static void destroy_context(DeviceContext* c) {
   cudaFree(c->dev_error);
   cudaFree(c->split_partials);
   cudaFreeHost(c->state_host);
+  cudaFreeHost(c->state_ahead);
+  for (int i = 0; i < 2; ++i)
+    if (c->state_ev[i]) cudaEventDestroy(c->state_ev[i]);
   cudaStreamDestroy(c->stream);
   delete c;
 }

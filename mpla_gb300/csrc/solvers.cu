@@ -530,8 +530,32 @@ int run_loop(DeviceContext* c, Matvec& A, SolverState* st_dev, const SolveOption
           cached = cached_graph(c, *cache_key);
         }
       }
-      MGB_CUDA(cudaGraphLaunch(cached ? cached->exec : g_chunk.exec, s));
-      count_launches(cached ? cached->kernels : g_chunk.kernels);
+      cudaGraphExec_t exec = cached ? cached->exec : g_chunk.exec;
+      const long long kernels = cached ? cached->kernels : g_chunk.kernels;
+      MGB_CUDA(cudaGraphLaunch(exec, s));
+      count_launches(kernels);
+      if (!hist_dev && o.checkpoint_every <= 0 && h.k >= 2 * kChunk) {
+        // A long solve without printing or checkpoints: keep the next chunk
+        // queued while the host reads the state of the previous one, so the
+        // GPU never waits for the host between chunks.  Iterations after
+        // convergence return at once (the done flag), so the one queued
+        // chunk that follows the last costs only its empty launches.
+        int i = 0;
+        MGB_CUDA(cudaMemcpyAsync(&c->state_ahead[0], st_dev, sizeof(SolverState), cudaMemcpyDeviceToHost, s));
+        MGB_CUDA(cudaEventRecord(c->state_ev[0], s));
+        for (;;) {
+          MGB_CUDA(cudaGraphLaunch(exec, s));
+          count_launches(kernels);
+          MGB_CUDA(cudaMemcpyAsync(&c->state_ahead[(i + 1) & 1], st_dev, sizeof(SolverState),
+                                   cudaMemcpyDeviceToHost, s));
+          MGB_CUDA(cudaEventRecord(c->state_ev[(i + 1) & 1], s));
+          MGB_CUDA(cudaEventSynchronize(c->state_ev[i & 1]));
+          if (c->state_ahead[i & 1].done) break;
+          ++i;
+        }
+        MGB_CUDA(cudaStreamSynchronize(s));
+        return MGB_OK;
+      }
     } else {
       if (!g_one.exec) MGB_TRY(capture_iterations(s, 1, one_iter, &g_one));
       for (int i = 0; i < todo; ++i) {
