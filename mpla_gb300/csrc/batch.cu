@@ -1077,7 +1077,19 @@ static WorkQueue make_queue(const BatchItem* items, int* counters, int cls, int 
 }
 
 template <int DIM, int R>
-static void launch_mv32(const WorkQueue& q, const BatchSys* sys, int rpt, int grid, cudaStream_t s) {
+static void launch_mv32(const WorkQueue& q, const BatchSys* sys, int rpt, int sms, cudaStream_t s) {
+  // persistent grid: as many CTAs as fit on every SM at once (the light
+  // variants hold up to 16 CTAs per SM, the R = 8 four-row one 4), so that
+  // the latency of each item's dependent chains is hidden by other CTAs
+  static int per_sm[2] = {0, 0};
+  int& occ = per_sm[rpt == 4 ? 1 : 0];
+  if (occ == 0) {
+    int b = 0;
+    if (rpt == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_bmv32<DIM, R, 4>, kTile, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_bmv32<DIM, R, 2>, kTile, 0);
+    occ = b > 0 ? b : 4;
+  }
+  const int grid = occ * sms;
   if (rpt == 4) k_bmv32<DIM, R, 4><<<grid, kTile, 0, s>>>(q, sys);
   else k_bmv32<DIM, R, 2><<<grid, kTile, 0, s>>>(q, sys);
 }
@@ -1102,8 +1114,7 @@ static void launch_mv32(const WorkQueue& q, const BatchSys* sys, int rpt, int gr
 int BatchEngine::enqueue_mv32(int cls, int rpt, cudaStream_t s) {
   const int list = rpt == 4 ? kListRpt4 : kListRpt2;
   const WorkQueue q = make_queue(items_[list][cls], counters_, cls, Q_MV32, list);
-  const int grid = 4 * c_->num_sms;
-#define MGB_MV32(D, R) launch_mv32<D, R>(q, dev_sys_, rpt, grid, s)
+#define MGB_MV32(D, R) launch_mv32<D, R>(q, dev_sys_, rpt, c_->num_sms, s)
   MGB_CLASS_SWITCH(cls, MGB_MV32)
 #undef MGB_MV32
   count_launches(1);
