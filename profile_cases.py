@@ -14,6 +14,7 @@ that ends by itself (a few hundred MB on the device at most):
   python profile_cases.py batch_trace # all 512 batch systems to 1e-10, per-replay times
   python profile_cases.py batch512    # 16 timed steps of all 512 batch systems
   python profile_cases.py serving_sweep  # the serving configuration, 3 rates x ~32 requests
+  python profile_cases.py serving_sweep 0.2,0.4 32  # chosen rates and requests per rate
   python profile_cases.py all
 
 Prints the CUDA-event time per launch of each case.
@@ -269,6 +270,14 @@ CASES = {"dgemv": case_dgemv, "gauss_f64": case_gauss_f64, "gauss_mixed": case_g
 def main(argv):
     mg.init(0)
     long_cases = ("mixed_c3", "batch128", "batch128_solve", "batch_trace", "batch512", "serving_sweep")
+    if argv and argv[0] == "serving_sweep" and len(argv) > 1:
+        # serving_sweep RATES [PER_RATE]: e.g. serving_sweep 0.2,0.4 24
+        rates = tuple(float(r) for r in argv[1].split(","))
+        per_rate = int(argv[2]) if len(argv) > 2 else 32
+        case_serving_sweep(rates=rates, per_rate=per_rate,
+                           out=f"gpurun_out/serving_sweep_{argv[1].replace(',', '_')}.json")
+        mg.synchronize()
+        return
     names = [k for k in CASES if k not in long_cases] if (not argv or argv[0] == "all") else argv
     for name in names:
         CASES[name]()
