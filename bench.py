@@ -10,15 +10,21 @@ vectors, dots, scalars and FP64 true-residual replacement).  The plain FP64
 CG on the same system is timed on a bounded sample of iterations (a full
 FP64 solve takes tens of minutes on GB300's FP64 pipe) and reported beside it.
 
-  value   solves/s with points, b and x resident in HBM (device-timed)
-  e2e     the same solve through mgb_cg_gauss_host from pinned host buffers
-          (host->device copies of points, b, x0 and the copy of x back inside
-          the timed region)
+  value     solves/s with points, b and x resident in HBM (device-timed)
+  e2e       the same solve through mgb_cg_gauss_host from pinned host buffers
+            (host->device copies of points, b, x0 and the copy of x back
+            inside the timed region)
+  dense     the dense configuration: FP64 CG solves/s and the dgemv, n = 4096
+  batched   all 512 systems of the batch configuration to relres 1e-10, with
+            plain FP64 extrapolated from per-step times and an iteration ratio
+  serving   continuous batching at three arrival rates (requests up to
+            n = 8192; profile_cases.py serving_sweep runs the full sizes)
 
 ``--impl reference`` times the reference MPLA (compiled from its sources into
 oracle/_ref by oracle/build_ref.py) on the same system through its own API:
 FP64 CG with the Gaussian system_assembler plugin, on a bounded sample of
-iterations.  Under torchrun every rank runs its own replica (the path does
+iterations, and the dense configuration (mpla_dgemv, its cublasDgemv call,
+the dense CG).  Under torchrun every rank runs its own replica (the path does
 not shard); rank 0 prints the JSON line.
 """
 from __future__ import annotations
