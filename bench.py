@@ -15,6 +15,8 @@ FP64 solve takes tens of minutes on GB300's FP64 pipe) and reported beside it.
             (host->device copies of points, b, x0 and the copy of x back
             inside the timed region)
   dense     the dense configuration: FP64 CG solves/s and the dgemv, n = 4096
+  mixed_c3  the mixed configuration's matvec (n = 131072, d = 3) against the
+            SFU peak
   batched   all 512 systems of the batch configuration to relres 1e-10, with
             plain FP64 extrapolated from per-step times and an iteration ratio
   serving   continuous batching at three arrival rates (requests up to
@@ -194,6 +196,28 @@ def cpu_baseline(points_scaled: np.ndarray, nugget: float, iterations: int, budg
 
 
 # ------------------------------------------------------- secondary sections
+def bench_mixed_c3(mg, stream, sms: int, sm_mhz: float) -> dict:
+    """The mixed-precision configuration's operator (n = 131072 points
+    U[0,1]^3, l = 0.08, nugget 1e-4): time of one mixed matvec (20 launches,
+    CUDA events) and its rate against the SFU peak.  A full solve of this
+    system takes about a minute; its record is a profile case
+    (profile_cases.py mixed_c3), not a bench step."""
+    from mpla_gb300 import synth
+
+    prob = synth.config_gauss_mixed(0)
+    n = prob.n
+    dp = mg.GaussPoints(prob.scaled())
+    dxr = mg.DeviceArray.from_numpy(np.random.default_rng(0).standard_normal(n))
+    dy = mg.DeviceArray(n)
+    ms = mg.time_gauss_matvec(dp, NUGGET, mg.PREC_MIXED, dxr.ptr, dy.ptr, reps=20, stream=stream.cuda_stream)
+    evaluated = float(mg.gauss_mixed_work(dp))
+    rate = evaluated / (ms * 1e-3)
+    peak = SFU_EX2_PER_CLK_SM * sms * sm_mhz * 1e6
+    return {"workload": "mixed matvec, n=131072, points U[0,1]^3, l=0.08, nugget 1e-4",
+            "matvec_ms": ms, "evaluated_per_launch": evaluated, "ex2_per_s": rate, "sfu_frac": rate / peak,
+            "algorithmic_entries_per_s": float(n) * n / (ms * 1e-3)}
+
+
 def bench_dense(mg, torch, stream, hbm_peak_gbs: float | None) -> dict:
     """Dense FP64 CG (n = 4096, A = M^T M / n + I, b = 1, relres 1e-10) and
     the dgemv on the same A."""
@@ -483,6 +507,8 @@ def run_ours(args, world, rank, local):
     if not args.no_dense:
         extra["dense"] = bench_dense(mg, torch, stream, measured_peak("hbm_gbs"))
         progress("dense done")
+        extra["mixed_c3"] = bench_mixed_c3(mg, stream, sms, sm_mhz)
+        progress("mixed C3 matvec done")
     if not args.no_batched:
         extra["batched"] = bench_batched(mg, args.batch_systems)
         progress("batched done")
