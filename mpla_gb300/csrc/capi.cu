@@ -29,7 +29,7 @@ int GaussF64Matvec::init(DeviceContext* c, const GaussSystem& g, cudaStream_t s)
   if (symmetric_ok(g)) {
     SymF64* m = new SymF64();
     sym_ = m;
-    return m->init(c, g);
+    return m->init(c, g, s);
   }
   c_ = c;
   return prepare_scaled_coords(c, g, &sc_, s);

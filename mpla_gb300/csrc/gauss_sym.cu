@@ -19,25 +19,27 @@
 //                 + nugget x_i: a fixed order, so the product is
 //                 bit-reproducible.
 //   Entries exp(-s) with the table exponential (devutil.cuh) on the squared
-//   distance of the caller's coordinates; 15 FP64 operations per evaluated
-//   entry, 7.5 per matrix entry (d = 2).  Every pair is evaluated.
+//   distance of the caller's coordinates (copied once in k-d tile order);
+//   15 FP64 operations per evaluated entry, 7.5 per matrix entry (d = 2).
+//   Tile pairs whose entries are all below 2^-80 are left out (60 % of the
+//   pairs are evaluated at n = 65536, d = 2, l = 0.05).
 //
 // FP32 (the mixed CG's operator, MGB_MIXED_SIMT):
 //   group kernel  one CTA per column tile and group of 4 row tiles, packed
-//                 f32x2 arithmetic, tile pairs whose entries are all below
-//                 2^-40 left out (see the kernel);
+//                 f32x2 arithmetic on (row, column pair) operands, tile
+//                 pairs whose entries are all below 2^-40 left out (see the
+//                 kernel);
 //   reduce kernel row slots of the near column tiles and the column slots of
 //                 the groups, in a fixed order.
 //   Points are in k-d tile order (compact tiles, kd_tile_perm) and rounded
 //   to FP32 once per point, so the FP32 operator is the Gaussian kernel
 //   matrix of a slightly perturbed point set and stays symmetric positive
-//   definite.  (A
-//   per-tile-pair centring, with the difference of the two tile centres
-//   rounded once per pair, perturbs every tile pair differently; at
-//   n = 65536 that operator made the mixed solve stagnate at relres 1.4e-10,
-//   so coordinates are global.)  Exponentials on the SFU (ex2.approx, with
-//   coordinates pre-scaled by sqrt(log2 e)).  About 8 issue slots and 1 MUFU
-//   per evaluated entry.
+//   definite.  (A per-tile-pair centring, with the difference of the two
+//   tile centres rounded once per pair, perturbs every tile pair
+//   differently; at n = 65536 that operator made the mixed solve stagnate at
+//   relres 1.4e-10, so coordinates are global.)  Exponentials on the SFU
+//   (ex2.approx, with coordinates pre-scaled by sqrt(log2 e)).  About 3.5
+//   issue slots of packed arithmetic and 1 MUFU per evaluated entry (d = 2).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -62,32 +64,6 @@ __device__ __forceinline__ float ex2_approx(float v) {
   float r;
   asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(v));
   return r;
-}
-
-// tile pair index p -> (I, J), I <= J, enumerating the upper triangle row by
-// row: p = I*T - I*(I-1)/2 + (J - I).  FP32 estimate of I (SFU sqrt) and
-// exact integer correction: no FP64 work (GB300's FP64 pipe is scarce).
-__device__ __forceinline__ void pair_of(long long p, int T, int* I, int* J) {
-  // I = largest i with start(i) <= p, start(i) = i*T - i*(i-1)/2
-  const float tt = 2.0f * (float)T + 1.0f;
-  const float disc = fmaxf(tt * tt - 8.0f * (float)p, 0.0f);
-  int i = (int)((tt - sqrtf(disc)) * 0.5f);
-  if (i < 0) i = 0;
-  if (i > T - 1) i = T - 1;
-  auto start = [&](long long k) { return k * T - k * (k - 1) / 2; };
-  while (i > 0 && start(i) > p) --i;
-  while (i + 1 < T && start(i + 1) <= p) ++i;
-  *I = i;
-  *J = i + (int)(p - start(i));
-}
-
-// (I, J) of pair p computed once per CTA and broadcast through shared memory.
-__device__ __forceinline__ void cta_pair(long long p, int T, int* I, int* J) {
-  __shared__ int s_ij[2];
-  if (threadIdx.x == 0) pair_of(p, T, &s_ij[0], &s_ij[1]);
-  __syncthreads();
-  *I = s_ij[0];
-  *J = s_ij[1];
 }
 
 // Write the CTA's row sums (acc_r, one per thread row) and column sums.
@@ -129,12 +105,16 @@ __global__ void __launch_bounds__(kThreads) sym_f64_pair_kernel(int n, int T, co
                                                                 const double* __restrict__ c1,
                                                                 const double* __restrict__ c2,
                                                                 const double* __restrict__ x,
+                                                                const int* __restrict__ perm,
                                                                 const double* __restrict__ table_g,
-                                                                double* __restrict__ S, long long npairs,
+                                                                double* __restrict__ S,
+                                                                const int2* __restrict__ pairs, int npairs,
                                                                 const int* __restrict__ skip) {
-  // A fixed grid strides over the tile pairs, so that a launch whose skip
-  // flag is set (the mixed CG's true-residual node on most iterations)
-  // costs a few thousand CTA starts, not one per tile pair.
+  // A fixed grid strides over the list of near tile pairs (I <= J), so that
+  // a launch whose skip flag is set (the mixed CG's true-residual node on
+  // most iterations) costs a few hundred CTA starts, not one per tile pair.
+  // Coordinates are in tile order, padded to whole tiles; x is the caller's,
+  // read through perm (tile position -> caller index).
   if (skip && *skip) return;
   // the exp table is dead once a pair's entries are evaluated; the column
   // reduction buffer (16 x 128 doubles) reuses its storage, and the table is
@@ -144,19 +124,17 @@ __global__ void __launch_bounds__(kThreads) sym_f64_pair_kernel(int n, int T, co
   __shared__ double sxv[2][kB];
   double* colbuf = table;
   static_assert(16 * kB <= kExpTableSize, "column buffer must fit in the table storage");
-  for (long long pair = blockIdx.x; pair < npairs; pair += gridDim.x) {
-  int I, J;
+  for (int pair = blockIdx.x; pair < npairs; pair += gridDim.x) {
+  const int2 ij = pairs[pair];
+  const int I = ij.x, J = ij.y;
   __syncthreads();  // the previous pair's column reduction is done with colbuf
-  cta_pair(pair, T, &I, &J);
   for (int i = threadIdx.x; i < kExpTableSize; i += kThreads) table[i] = table_g[i];
   for (int t = threadIdx.x; t < 2 * kB; t += kThreads) {
     const int side = t / kB, k = t % kB;
     const int g = (side ? J : I) * kB + k;
-    const bool in = g < n;
-    const int gc = in ? g : n - 1;
 #pragma unroll
-    for (int d = 0; d < DIM; ++d) sp[side][d][k] = (d == 0 ? c0 : (d == 1 ? c1 : c2))[gc];
-    sxv[side][k] = in ? x[g] : 0.0;
+    for (int d = 0; d < DIM; ++d) sp[side][d][k] = (d == 0 ? c0 : (d == 1 ? c1 : c2))[g];
+    sxv[side][k] = g < n ? x[perm[g]] : 0.0;
   }
   __syncthreads();
   const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
@@ -198,9 +176,11 @@ __global__ void __launch_bounds__(kThreads) sym_f64_pair_kernel(int n, int T, co
   }
 }
 
-// y_i = sum_K S[tile(i)][K][i % B] + nugget x_i
-__global__ void sym_f64_reduce_kernel(int n, int T, const double* __restrict__ S, const double* __restrict__ x,
-                                      double nugget, double* __restrict__ y, const int* __restrict__ skip) {
+// y[perm[i]] = sum_K S[tile(i)][K][i % B] + nugget x[perm[i]], the slots in
+// tile order (the slots of far pairs hold zeros)
+__global__ void sym_f64_reduce_kernel(int n, int T, const double* __restrict__ S, const int* __restrict__ perm,
+                                      const double* __restrict__ x, double nugget, double* __restrict__ y,
+                                      const int* __restrict__ skip) {
   if (skip && *skip) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -209,7 +189,8 @@ __global__ void sym_f64_reduce_kernel(int n, int T, const double* __restrict__ S
   double s = 0.0;
 #pragma unroll 4
   for (int k = 0; k < T; ++k) s += __ldcg(p + (long long)k * kB);
-  y[i] = fma(nugget, x[i], s);
+  const int o = perm[i];
+  y[o] = fma(nugget, x[o], s);
 }
 
 // ----------------------------------------------------------------- FP32
@@ -264,19 +245,25 @@ __device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
 }
 
 // One CTA takes a column tile J and a group of up to kGroup row tiles
-// I = kGroup*g .. min(kGroup*g + kGroup - 1, J).  The column tile is staged
-// once in shared memory with each value twice over, so that one 128-bit load
-// gives packed operands: cq[t] = {x, x, y, y}, cw[t] = {z, z, x_t, x_t} (x_t
-// the FP32 vector entry).  Warp w owns columns 32w .. 32w+31 and, for every
-// row tile of the group, lane l owns rows l, l+32, l+64, l+96, paired as
-// (l, l+32) and (l+64, l+96).  Per pair of entries: packed subtractions, a
-// packed multiply and FMA for the squared distance, two MUFU.EX2, a packed
-// FMA into the row sums and one into the column partial.  Column partials
-// accumulate over the whole group in registers, and one butterfly
-// reduce-scatter per CTA (31 shuffles and adds per lane) leaves lane l with
-// column 32w + l complete (the warp saw every row of the group).  The
-// diagonal tile I = J is evaluated in full for its row sums and adds nothing
-// to the column partials (its row weights are zero there), so every
+// I = kGroup*g .. min(kGroup*g + kGroup - 1, J).  Warp w owns columns
+// 32w .. 32w+31 and, for every row tile of the group, lane l owns rows l,
+// l+32, l+64, l+96.  A packed pair is one row and two adjacent columns
+// (b, b+1): the column tile is staged once in shared memory as column pairs,
+// cxy[t] = {x_2t, x_2t+1, y_2t, y_2t+1} and czw[t] = {z_2t, z_2t+1, w_2t,
+// w_2t+1} (w the FP32 vector entry), so one broadcast 128-bit load gives the
+// packed column operands of 8 entries of a lane.  Per pair of entries: packed
+// subtractions, a packed multiply and FMA for the squared distance, two
+// MUFU.EX2, a packed FMA into the row's two half-sums (even and odd columns)
+// and a packed FMA into the pair of column partials -- both halves of every
+// packed accumulator belong to one sum, so no repacking per entry.  (Pairing
+// two rows of one column instead needs a MOV and an FADD per column to fold
+// the column halves: 7 issue slots per entry against 6.25, and 0.269 against
+// 0.213 ms for the whole matvec at n = 65536, d = 2 on GB300.)
+// Column partials accumulate over the whole group in registers, and one
+// butterfly reduce-scatter per CTA (31 shuffles and adds per lane) leaves
+// lane l with column 32w + l complete (the warp saw every row of the group).
+// The diagonal tile I = J is evaluated in full for its row sums and adds
+// nothing to the column partials (its row weights are zero there), so every
 // unordered pair of points counts once per direction.  Row sums of each row
 // tile combine the 4 warps in shared memory in warp order.
 //
@@ -287,15 +274,10 @@ __device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
 // the nugget.  The CTA map lists only groups with a near row tile, and a
 // 4-bit mask per CTA marks which of its row tiles are near; the slots of
 // far pairs are zeroed once and never written.
-//
-// SCALAR (d <= 2): the squared distance in scalar FP32 with the negation
-// folded into the FMA, the column values read as scalars from the same
-// staging; fewer registers (94 against 102) and no repacking between the
-// packed and scalar forms around the MUFU.EX2 operands.
 constexpr int kGroup = 4;
 constexpr double kFarLog2 = 40.0;
 
-template <int DIM, bool SCALAR>
+template <int DIM>
 __global__ void __launch_bounds__(kF32Threads) sym_f32_group_kernel(int n, int T, int GT,
                                                                     const int2* __restrict__ map,
                                                                     const float4* __restrict__ pts,
@@ -304,8 +286,8 @@ __global__ void __launch_bounds__(kF32Threads) sym_f32_group_kernel(int n, int T
                                                                     float* __restrict__ Scol,
                                                                     const int* __restrict__ skip) {
   if (skip && *skip) return;
-  __shared__ ulonglong2 cq[kB];  // {x, x} {y, y} as packed pairs
-  __shared__ ulonglong2 cw[kB];  // {z, z} {x_t, x_t}
+  __shared__ float4 cxy[kB / 2];  // {x_2t, x_2t+1, y_2t, y_2t+1}
+  __shared__ float4 czw[kB / 2];  // {z_2t, z_2t+1, w_2t, w_2t+1}
   __shared__ float rowacc[kGroup][4][kB];
   const int2 jm = map[blockIdx.x];
   const int J = jm.x, g = jm.y & 0xFFFF, near = jm.y >> 16;
@@ -315,103 +297,75 @@ __global__ void __launch_bounds__(kF32Threads) sym_f32_group_kernel(int n, int T
     const int gi = J * kB + t;
     const float4 p = pts[gi];  // padded to whole tiles
     const float w = gi < n ? xf[gi] : 0.f;
-    cq[t] = make_ulonglong2(f2_pack(p.x, p.x), f2_pack(p.y, p.y));
-    cw[t] = make_ulonglong2(f2_pack(p.z, p.z), f2_pack(w, w));
+    float* fxy = reinterpret_cast<float*>(cxy);
+    float* fzw = reinterpret_cast<float*>(czw);
+    const int o = 4 * (t >> 1) + (t & 1);
+    fxy[o] = p.x;
+    fxy[o + 2] = p.y;
+    fzw[o] = p.z;
+    fzw[o + 2] = w;
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  float col[32];
+  uint64_t col2[16];  // columns (2b, 2b+1) of the warp's 32
 #pragma unroll
-  for (int b = 0; b < 32; ++b) col[b] = 0.f;
+  for (int b = 0; b < 16; ++b) col2[b] = 0ull;
 #pragma unroll 1
   for (int I = I0; I <= I1; ++I) {
     if (!((near >> (I - I0)) & 1)) continue;
-    uint64_t rx[2], ry[2], rz[2], xi2[2], acc[2];
     const bool diag = I == J;
+    float rx[4], ry[4], rz[4];
+    uint64_t xi2[4], acc2[4];
 #pragma unroll
-    for (int q = 0; q < 2; ++q) {
-      const int r0 = I * kB + lane + 64 * q, r1 = r0 + 32;
-      const float4 a = pts[r0], b = pts[r1];
-      const float wa = (!diag && r0 < n) ? xf[r0] : 0.f;
-      const float wb = (!diag && r1 < n) ? xf[r1] : 0.f;
-      rx[q] = f2_pack(a.x, b.x);
-      ry[q] = f2_pack(a.y, b.y);
-      rz[q] = f2_pack(a.z, b.z);
-      xi2[q] = f2_pack(wa, wb);
-      acc[q] = 0ull;  // +0.0f in both halves
+    for (int a = 0; a < 4; ++a) {
+      const int r = I * kB + lane + 32 * a;
+      const float4 p = pts[r];
+      const float w = (!diag && r < n) ? xf[r] : 0.f;
+      rx[a] = p.x;
+      ry[a] = p.y;
+      rz[a] = p.z;
+      xi2[a] = f2_pack(w, w);
+      acc2[a] = 0ull;  // +0.0f in both halves
     }
 #pragma unroll
-    for (int b = 0; b < 32; ++b) {
-      uint64_t qx, qy, qz, qw;
-      float qxs = 0.f, qys = 0.f;
-      if (SCALAR && DIM <= 2) {
-        // one 16-byte load {x, x, y, y}: the scalar coordinates, and {x_t, x_t}
-        const float4 q4 = reinterpret_cast<const float4*>(cq)[32 * warp + b];
-        qxs = q4.x;
-        qys = q4.z;
-        qx = qy = qz = 0ull;
-        qw = reinterpret_cast<const ulonglong2*>(cw)[32 * warp + b].y;
-      } else {
-        const ulonglong2 q2 = cq[32 * warp + b];
-        const ulonglong2 w2 = cw[32 * warp + b];
-        qx = q2.x;
-        qy = q2.y;
-        qz = w2.x;
-        qw = w2.y;
-      }
-      uint64_t c2 = f2_pack(col[b], 0.f);
+    for (int b = 0; b < 16; ++b) {
+      const float4 P = cxy[16 * warp + b];
+      const float4 Z = czw[16 * warp + b];
+      const uint64_t wq = f2_pack(Z.z, Z.w);
+      uint64_t c2 = col2[b];
 #pragma unroll
-      for (int q = 0; q < 2; ++q) {
-        float ns0, ns1;  // minus the squared distances of the two rows
-        if (SCALAR && DIM <= 2) {
-          // scalar FP32 with the negation folded into the FMA: fewer
-          // registers and no repacking between the packed and scalar forms
-          float ax, bx, ay, by;
-          f2_unpack(rx[q], ax, bx);
-          const float dxa = ax - qxs, dxb = bx - qxs;
-          if (DIM == 1) {
-            ns0 = -dxa * dxa;
-            ns1 = -dxb * dxb;
-          } else {
-            f2_unpack(ry[q], ay, by);
-            const float dya = ay - qys, dyb = by - qys;
-            ns0 = fmaf(-dxa, dxa, -(dya * dya));
-            ns1 = fmaf(-dxb, dxb, -(dyb * dyb));
-          }
+      for (int a = 0; a < 4; ++a) {
+        const uint64_t dx = f2_sub(f2_pack(rx[a], rx[a]), f2_pack(P.x, P.y));
+        uint64_t s2;
+        if (DIM == 1) {
+          s2 = f2_mul(dx, dx);
         } else {
-          const uint64_t dx = f2_sub(rx[q], qx);
-          uint64_t s2;
-          if (DIM == 1) {
-            s2 = f2_mul(dx, dx);
-          } else if (DIM == 2) {
-            const uint64_t dy = f2_sub(ry[q], qy);
+          const uint64_t dy = f2_sub(f2_pack(ry[a], ry[a]), f2_pack(P.z, P.w));
+          if (DIM == 2) {
             s2 = f2_fma(dx, dx, f2_mul(dy, dy));
           } else {
-            const uint64_t dy = f2_sub(ry[q], qy);
-            const uint64_t dz = f2_sub(rz[q], qz);
+            const uint64_t dz = f2_sub(f2_pack(rz[a], rz[a]), f2_pack(Z.x, Z.y));
             s2 = f2_fma(dx, dx, f2_fma(dy, dy, f2_mul(dz, dz)));
           }
-          float s0, s1;
-          f2_unpack(s2, s0, s1);
-          ns0 = -s0;
-          ns1 = -s1;
         }
-        const uint64_t e2 = f2_pack(ex2_approx(ns0), ex2_approx(ns1));
-        acc[q] = f2_fma(e2, qw, acc[q]);
-        c2 = f2_fma(e2, xi2[q], c2);
+        float s0, s1;
+        f2_unpack(s2, s0, s1);
+        const uint64_t e2 = f2_pack(ex2_approx(-s0), ex2_approx(-s1));
+        acc2[a] = f2_fma(e2, wq, acc2[a]);
+        c2 = f2_fma(e2, xi2[a], c2);
       }
-      float c0, c1;
-      f2_unpack(c2, c0, c1);
-      col[b] = c0 + c1;
+      col2[b] = c2;
     }
 #pragma unroll
-    for (int q = 0; q < 2; ++q) {
-      float a0, a1;
-      f2_unpack(acc[q], a0, a1);
-      rowacc[I - I0][warp][lane + 64 * q] = a0;
-      rowacc[I - I0][warp][lane + 64 * q + 32] = a1;
+    for (int a = 0; a < 4; ++a) {
+      float lo, hi;
+      f2_unpack(acc2[a], lo, hi);
+      rowacc[I - I0][warp][lane + 32 * a] = lo + hi;
     }
   }
+  float col[32];
+#pragma unroll
+  for (int b = 0; b < 16; ++b) f2_unpack(col2[b], col[2 * b], col[2 * b + 1]);
   warp_reduce_scatter32(col, lane);
   Scol[((long long)J * GT + g) * kB + 32 * warp + lane] = col[0];
   __syncthreads();
@@ -432,38 +386,54 @@ __global__ void sym_f32_gather_kernel(int n, const int* __restrict__ perm, const
 }
 
 // y[perm[i]] = nugget x + row slots of the near column tiles J >= I (a
-// per-row-tile list) + column slots (groups of the column tile I): FP32
-// groups of 16 slots added in FP64, in a fixed order.
-__global__ void sym_f32_reduce_kernel(int n, int T, int GT, const float* __restrict__ Srow,
-                                      const float* __restrict__ Scol, const int* __restrict__ near_off,
-                                      const int* __restrict__ near_J, const int* __restrict__ perm,
-                                      const double* __restrict__ x, double nugget, double* __restrict__ y,
-                                      const int* __restrict__ skip) {
+// per-row-tile list) + column slots (groups of the column tile I): FP32 sums
+// of 8 consecutive slots added in FP64, in a fixed order.  kRedSplit threads
+// share a row (warp q of a CTA takes the 8-slot groups q, q + kRedSplit, ...
+// of 32 consecutive rows, so every load of a warp is one 128-byte line), and
+// their FP64 sums combine in thread order: with one thread per row the loads
+// of a row were too few in flight to cover their latency (0.150 ms for the
+// slots of n = 131072, d = 3, which stream from HBM at 6.7 TB/s in 0.03 ms).
+constexpr int kRedRows = 32, kRedSplit = 8, kRedGroup = 8;
+
+__global__ void __launch_bounds__(kRedRows * kRedSplit) sym_f32_reduce_kernel(
+    int n, int T, int GT, const float* __restrict__ Srow, const float* __restrict__ Scol,
+    const int* __restrict__ near_off, const int* __restrict__ near_J, const int* __restrict__ perm,
+    const double* __restrict__ x, double nugget, double* __restrict__ y, const int* __restrict__ skip) {
   if (skip && *skip) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const int I = i / kB, r = i % kB;
+  __shared__ double part[kRedSplit][kRedRows];
+  const int rl = threadIdx.x & (kRedRows - 1), q = threadIdx.x / kRedRows;
+  const int i = blockIdx.x * kRedRows + rl;
   double s = 0.0;
-  const float* pr = Srow + (long long)I * T * kB + r;
-  const int k0 = near_off[I], k1 = near_off[I + 1];
-  for (int a = k0; a < k1; a += 16) {
-    const int b = min(k1, a + 16);
-    float gsum = 0.f;
+  if (i < n) {
+    const int I = i / kB, r = i % kB;
+    const float* pr = Srow + (long long)I * T * kB + r;
+    const int k0 = near_off[I], k1 = near_off[I + 1];
+    for (int a = k0 + kRedGroup * q; a < k1; a += kRedGroup * kRedSplit) {
+      const int b = min(k1, a + kRedGroup);
+      float gsum = 0.f;
 #pragma unroll 8
-    for (int k = a; k < b; ++k) gsum += __ldcg(pr + (long long)__ldg(&near_J[k]) * kB);
-    s += (double)gsum;
-  }
-  const float* pc = Scol + (long long)I * GT * kB + r;
-  const int ng = I / kGroup + 1;
-  for (int g0 = 0; g0 < ng; g0 += 16) {
-    const int g1 = min(ng, g0 + 16);
-    float gsum = 0.f;
+      for (int k = a; k < b; ++k) gsum += __ldcg(pr + (long long)__ldg(&near_J[k]) * kB);
+      s += (double)gsum;
+    }
+    const float* pc = Scol + (long long)I * GT * kB + r;
+    const int ng = I / kGroup + 1;
+    for (int g0 = kRedGroup * q; g0 < ng; g0 += kRedGroup * kRedSplit) {
+      const int g1 = min(ng, g0 + kRedGroup);
+      float gsum = 0.f;
 #pragma unroll 8
-    for (int g = g0; g < g1; ++g) gsum += __ldcg(pc + (long long)g * kB);
-    s += (double)gsum;
+      for (int g = g0; g < g1; ++g) gsum += __ldcg(pc + (long long)g * kB);
+      s += (double)gsum;
+    }
   }
-  const int o = perm[i];
-  y[o] = fma(nugget, x[o], s);
+  part[q][rl] = s;
+  __syncthreads();
+  if (q == 0 && i < n) {
+    double t = part[0][rl];
+#pragma unroll
+    for (int k = 1; k < kRedSplit; ++k) t += part[k][rl];
+    const int o = perm[i];
+    y[o] = fma(nugget, x[o], t);
+  }
 }
 
 // Morton (Z-order) key of a point quantised to 21 bits per axis.
@@ -562,31 +532,92 @@ std::vector<int> morton_perm(const std::vector<double>& h, int n, int dim) {
 }
 
 SymF64::~SymF64() {
-  if (c_) pool_free(c_, S_);
+  if (c_) {
+    pool_free(c_, S_);
+    pool_free(c_, pts_);
+  }
 }
 
-int SymF64::init(DeviceContext* c, const GaussSystem& g) {
+// Tile pairs whose entries are all below 2^-80 are left out of the FP64
+// operator: summed over all n <= 2^31 columns they change a row by less than
+// 2^-49 |x|_max, and in practice (the entries fall off as exp(-s) beyond
+// the cut) by far less than one rounding of the row's FP64 sum.
+constexpr double kFarF64 = 80.0 * 0.69314718055994531;  // exp(-s) < 2^-80
+
+int SymF64::init(DeviceContext* c, const GaussSystem& g, cudaStream_t s) {
   if (g.rows != g.cols || g.row_offset || g.col_offset || g.dim < 1 || g.dim > 3 ||
       g.nugget_rule != MGB_NUGGET_DIAGONAL)
     return set_error(MGB_ERR_ARG, "symmetric FP64 matvec: square d<=3 systems with a diagonal nugget only");
   c_ = c;
   g_ = g;
-  T_ = sym_tiles(g.rows);
-  return pool_alloc(c, sizeof(double) * (size_t)T_ * T_ * kB, (void**)&S_);
+  const int n = g.rows, dim = g.dim;
+  T_ = sym_tiles(n);
+  std::vector<double> h((size_t)n * dim);
+  for (int d = 0; d < dim; ++d)
+    MGB_CUDA(cudaMemcpyAsync(h.data() + (size_t)d * n, g.coords[d], sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  MGB_CUDA(cudaStreamSynchronize(s));
+  const std::vector<int> perm = kd_tile_perm(h, n, dim, kB);
+  const size_t np = (size_t)T_ * kB;
+  std::vector<double> pts(3 * np, 0.0);  // tile order, padded with zeros
+  for (int d = 0; d < dim; ++d)
+    for (int k = 0; k < n; ++k) pts[d * np + k] = h[(size_t)d * n + perm[k]];
+  std::vector<double> blo((size_t)3 * T_, 0.0), bhi((size_t)3 * T_, 0.0);
+  for (int t = 0; t < T_; ++t) {
+    const int b0 = t * kB, b1 = std::min(n, b0 + kB);
+    for (int d = 0; d < dim; ++d) {
+      double lo = 1e300, hi = -1e300;
+      for (int k = b0; k < b1; ++k) {
+        lo = std::min(lo, pts[d * np + k]);
+        hi = std::max(hi, pts[d * np + k]);
+      }
+      blo[3 * t + d] = lo;
+      bhi[3 * t + d] = hi;
+    }
+  }
+  std::vector<int2> pairs;
+  for (int I = 0; I < T_; ++I)
+    for (int J = I; J < T_; ++J) {
+      double d2 = 0.0;
+      for (int d = 0; d < dim; ++d) {
+        const double gap = std::max({0.0, blo[3 * J + d] - bhi[3 * I + d], blo[3 * I + d] - bhi[3 * J + d]});
+        d2 += gap * gap;
+      }
+      if (d2 <= kFarF64) pairs.push_back(make_int2(I, J));
+    }
+  if (pairs.size() > 0x7fffffffULL) return set_error(MGB_ERR_ARG, "system too large for one pair list");
+  npairs_ = (int)pairs.size();
+  auto up = [](size_t b) { return (b + 255) & ~size_t(255); };
+  const size_t b_pts = sizeof(double) * 3 * np, b_perm = sizeof(int) * (size_t)n;
+  const size_t b_pairs = sizeof(int2) * std::max<size_t>(1, pairs.size());
+  MGB_TRY(pool_alloc(c, up(b_pts) + up(b_perm) + up(b_pairs), (void**)&pts_));
+  perm_ = reinterpret_cast<int*>(reinterpret_cast<char*>(pts_) + up(b_pts));
+  pairs_ = reinterpret_cast<int2*>(reinterpret_cast<char*>(perm_) + up(b_perm));
+  MGB_CUDA(cudaMemcpyAsync(pts_, pts.data(), b_pts, cudaMemcpyHostToDevice, s));
+  MGB_CUDA(cudaMemcpyAsync(perm_, perm.data(), b_perm, cudaMemcpyHostToDevice, s));
+  if (!pairs.empty())
+    MGB_CUDA(cudaMemcpyAsync(pairs_, pairs.data(), sizeof(int2) * pairs.size(), cudaMemcpyHostToDevice, s));
+  const size_t b_slots = sizeof(double) * (size_t)T_ * T_ * kB;
+  MGB_TRY(pool_alloc(c, b_slots, (void**)&S_));
+  // slots of far pairs are never written: zero them once
+  MGB_CUDA(cudaMemsetAsync(S_, 0, b_slots, s));
+  MGB_CUDA(cudaStreamSynchronize(s));
+  return MGB_OK;
 }
 
 int SymF64::apply(const double* x, double* y, cudaStream_t s, const int* skip) {
-  const long long pairs = (long long)T_ * (T_ + 1) / 2;
-  const unsigned grid = (unsigned)std::min<long long>(pairs, 4LL * c_->num_sms);
-  const double* c0 = g_.coords[0];
-  const double* c1 = g_.dim > 1 ? g_.coords[1] : c0;
-  const double* c2 = g_.dim > 2 ? g_.coords[2] : c0;
+  const int n = g_.rows;
+  const size_t np = (size_t)T_ * kB;
+  const double* c0 = pts_;
+  const double* c1 = pts_ + np;
+  const double* c2 = pts_ + 2 * np;
+  const unsigned grid = (unsigned)std::max(1, std::min(npairs_, 4 * c_->num_sms));
+  const double* tab = c_->exp_table;
   switch (g_.dim) {
-    case 1: sym_f64_pair_kernel<1><<<grid, kThreads, 0, s>>>(g_.rows, T_, c0, c1, c2, x, c_->exp_table, S_, pairs, skip); break;
-    case 2: sym_f64_pair_kernel<2><<<grid, kThreads, 0, s>>>(g_.rows, T_, c0, c1, c2, x, c_->exp_table, S_, pairs, skip); break;
-    default: sym_f64_pair_kernel<3><<<grid, kThreads, 0, s>>>(g_.rows, T_, c0, c1, c2, x, c_->exp_table, S_, pairs, skip); break;
+    case 1: sym_f64_pair_kernel<1><<<grid, kThreads, 0, s>>>(n, T_, c0, c1, c2, x, perm_, tab, S_, pairs_, npairs_, skip); break;
+    case 2: sym_f64_pair_kernel<2><<<grid, kThreads, 0, s>>>(n, T_, c0, c1, c2, x, perm_, tab, S_, pairs_, npairs_, skip); break;
+    default: sym_f64_pair_kernel<3><<<grid, kThreads, 0, s>>>(n, T_, c0, c1, c2, x, perm_, tab, S_, pairs_, npairs_, skip); break;
   }
-  sym_f64_reduce_kernel<<<(g_.rows + 255) / 256, 256, 0, s>>>(g_.rows, T_, S_, x, g_.nugget, y, skip);
+  sym_f64_reduce_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, T_, S_, perm_, x, g_.nugget, y, skip);
   count_launches(2);
   MGB_CUDA(cudaGetLastError());
   return MGB_OK;
@@ -698,15 +729,13 @@ int SymF32::init(DeviceContext* c, const GaussSystem& g, cudaStream_t s) {
 int SymF32::apply(const double* x, double* y, cudaStream_t s, const int* skip) {
   sym_f32_gather_kernel<<<(n_ + 255) / 256, 256, 0, s>>>(n_, perm_, x, xf_, skip);
   const unsigned grid = (unsigned)ncta_;
-  // d <= 2: squared distances in scalar FP32 (5 % faster than the packed
-  // form at n = 65536, d = 2 on GB300: 0.288 against 0.304 ms); d = 3: packed
   switch (dim_) {
-    case 1: sym_f32_group_kernel<1, true><<<grid, kF32Threads, 0, s>>>(n_, T_, GT_, map_, pts_, xf_, S_, Scol_, skip); break;
-    case 2: sym_f32_group_kernel<2, true><<<grid, kF32Threads, 0, s>>>(n_, T_, GT_, map_, pts_, xf_, S_, Scol_, skip); break;
-    default: sym_f32_group_kernel<3, false><<<grid, kF32Threads, 0, s>>>(n_, T_, GT_, map_, pts_, xf_, S_, Scol_, skip); break;
+    case 1: sym_f32_group_kernel<1><<<grid, kF32Threads, 0, s>>>(n_, T_, GT_, map_, pts_, xf_, S_, Scol_, skip); break;
+    case 2: sym_f32_group_kernel<2><<<grid, kF32Threads, 0, s>>>(n_, T_, GT_, map_, pts_, xf_, S_, Scol_, skip); break;
+    default: sym_f32_group_kernel<3><<<grid, kF32Threads, 0, s>>>(n_, T_, GT_, map_, pts_, xf_, S_, Scol_, skip); break;
   }
-  sym_f32_reduce_kernel<<<(n_ + 255) / 256, 256, 0, s>>>(n_, T_, GT_, S_, Scol_, near_off_, near_J_, perm_, x,
-                                                          nugget_, y, skip);
+  sym_f32_reduce_kernel<<<(n_ + kRedRows - 1) / kRedRows, kRedRows * kRedSplit, 0, s>>>(
+      n_, T_, GT_, S_, Scol_, near_off_, near_J_, perm_, x, nugget_, y, skip);
   count_launches(3);
   MGB_CUDA(cudaGetLastError());
   return MGB_OK;

@@ -19,19 +19,26 @@ std::vector<int> morton_perm(const std::vector<double>& h, int n, int dim);
 // within the 2^-40 cut (13 % at n = 131072, d = 3, l = 0.08).
 std::vector<int> kd_tile_perm(const std::vector<double>& h, int n, int dim, int leaf);
 
-// FP64: the plain-CG operator.
+// FP64: the plain-CG operator (points in k-d tile order, tile pairs below
+// 2^-80 left out).
 class SymF64 : public Matvec {
  public:
   ~SymF64() override;
-  int init(DeviceContext* c, const GaussSystem& g);
+  int init(DeviceContext* c, const GaussSystem& g, cudaStream_t s);
   int apply(const double* x, double* y, cudaStream_t s, const int* skip) override;
   int n() const override { return g_.rows; }
+  // kernel entries one apply evaluates (each unordered near pair once)
+  long long evaluated() const { return (long long)npairs_ * 128LL * 128LL; }
 
  private:
   DeviceContext* c_ = nullptr;
   GaussSystem g_{};
   int T_ = 0;
-  double* S_ = nullptr;  // T x T x 128 slot partials
+  int npairs_ = 0;
+  double* S_ = nullptr;    // T x T x 128 slot partials
+  double* pts_ = nullptr;  // 3 x T*128 coordinates in tile order (one pool block with the rest)
+  int* perm_ = nullptr;    // tile position -> caller index
+  int2* pairs_ = nullptr;  // near tile pairs (I <= J)
 };
 
 // FP32 + SFU on points in k-d tile order (packed f32x2 arithmetic): the
