@@ -60,7 +60,7 @@ FP64_ITERATIONS_N65536 = 18958
 # the FP32 group kernel at n = 65536, d = 2, from one ncu capture of that
 # launch (points, slots and x stay in L2).  Not measured per run: ncu is not
 # run inside the benchmark.
-GROUP_KERNEL_DRAM_BYTES_N65536 = 1.462272e6 + 0.571648e6
+GROUP_KERNEL_DRAM_BYTES_N65536 = 1.441024e6 + 0.295936e6
 SFU_EX2_PER_CLK_SM = 32.0
 SMI_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -495,6 +495,7 @@ def run_ours(args, world, rank, local):
     mixed_rate = evaluated / (mixed_ms * 1e-3)
     sfu_peak = SFU_EX2_PER_CLK_SM * sms * sm_mhz * 1e6
     fp64_rate = entries / (f64_ms * 1e-3)
+    fp64_evaluated = float(mg.gauss_fp64_work(dp))   # entries one FP64 matvec evaluates
 
     iters_mixed = int(info.iterations)
     iters_fp64 = fp64_iterations(args, iters_mixed)
@@ -544,6 +545,7 @@ def run_ours(args, world, rank, local):
                 "d2h_bytes_per_step": int(8 * n)},
         "fp64": {"ms_per_iteration": fp_ms_per_iter, "sample_iterations": int(finfo.iterations + 1),
                  "matvec_ms": f64_ms, "entries_per_s": fp64_rate,
+                 "evaluated_per_launch": fp64_evaluated, "evaluated_per_s": fp64_evaluated / (f64_ms * 1e-3),
                  "iterations_assumed": iters_fp64,
                  "solves_per_s_est": fp64_solves_est,
                  "mixed_over_fp64": value / fp64_solves_est},
@@ -553,8 +555,9 @@ def run_ours(args, world, rank, local):
                      "traffic": GROUP_KERNEL_DRAM_BYTES_N65536 if (n == N_FULL and DIM == 2) else None,
                      "traffic_unit": "DRAM bytes per launch",
                      "traffic_source": "one ncu capture of this kernel at n=65536, d=2 (not measured in this run)",
-                     "per_unit": "1 evaluated kernel entry = 1 ex2 (+ ~7 FP32 issue slots); each unordered pair of "
-                                 "points evaluated once, tile pairs below 2^-40 skipped",
+                     "per_unit": "1 evaluated kernel entry = 1 ex2 (+ 6 FP32 lane operations in 3 packed FMA-pipe "
+                                 "instructions, d = 2); each unordered pair of points evaluated once, tile pairs "
+                                 "below 2^-40 skipped",
                      "evaluated_per_launch": evaluated, "algorithmic_entries_per_launch": entries,
                      "algorithmic_entries_per_s": entries / (mixed_ms * 1e-3), "matvec_ms": mixed_ms,
                      "peak_source": f"{SFU_EX2_PER_CLK_SM:.0f} ex2/clk/SM (the XU pipe peak ncu reports on GB300) "

@@ -173,6 +173,10 @@ int mgb_set_mixed_matvec(int kind);
  * each unordered pair once, tile pairs whose entries are all below 2^-40
  * left out (MGB_MIXED_SIMT).  The work figure of the roofline. */
 int mgb_gauss_mixed_work(int n, int dim, const double* const* coords_dev, long long* evaluated);
+/* Kernel entries one FP64 matvec of this system (diagonal nugget) evaluates:
+ * for d <= 3 each unordered pair once, tile pairs whose entries are all
+ * below 2^-80 left out; n^2 otherwise. */
+int mgb_gauss_fp64_work(int n, int dim, const double* const* coords_dev, long long* evaluated);
 int mgb_get_mixed_matvec(void);
 
 /* ------------------------------------------------------------ measurement */

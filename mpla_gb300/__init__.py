@@ -49,7 +49,7 @@ C_ABI_SYMBOLS = (
     "mgb_batch_create", "mgb_batch_add", "mgb_batch_run", "mgb_batch_run_async", "mgb_batch_wait", "mgb_batch_ready",
     "mgb_batch_finished", "mgb_batch_result",
     "mgb_batch_tuning", "mgb_batch_destroy",
-    "mgb_set_mixed_matvec", "mgb_get_mixed_matvec", "mgb_gauss_mixed_work",
+    "mgb_set_mixed_matvec", "mgb_get_mixed_matvec", "mgb_gauss_mixed_work", "mgb_gauss_fp64_work",
     "mgb_register_generic_device_code", "mgb_unregister_generic_device_code",
     "mgb_halton",
 )
@@ -128,6 +128,7 @@ _SIGS = {
     "mgb_set_mixed_matvec": (_I, [_I]),
     "mgb_get_mixed_matvec": (_I, []),
     "mgb_gauss_mixed_work": (_I, [_I, _I, _P, C.POINTER(C.c_longlong)]),
+    "mgb_gauss_fp64_work": (_I, [_I, _I, _P, C.POINTER(C.c_longlong)]),
 }
 
 
@@ -276,6 +277,13 @@ def gauss_mixed_work(pts: GaussPoints) -> int:
     """Kernel entries one mixed matvec of this system evaluates."""
     out = C.c_longlong()
     check(lib().mgb_gauss_mixed_work(pts.n, pts.dim, pts.coords, C.byref(out)))
+    return out.value
+
+
+def gauss_fp64_work(pts: GaussPoints) -> int:
+    """Kernel entries one FP64 matvec of this system evaluates."""
+    out = C.c_longlong()
+    check(lib().mgb_gauss_fp64_work(pts.n, pts.dim, pts.coords, C.byref(out)))
     return out.value
 
 

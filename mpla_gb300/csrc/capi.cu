@@ -29,9 +29,12 @@ int GaussF64Matvec::init(DeviceContext* c, const GaussSystem& g, cudaStream_t s)
   if (symmetric_ok(g)) {
     SymF64* m = new SymF64();
     sym_ = m;
-    return m->init(c, g, s);
+    MGB_TRY(m->init(c, g, s));
+    evaluated_ = m->evaluated();
+    return MGB_OK;
   }
   c_ = c;
+  evaluated_ = (long long)g.rows * g.cols;
   return prepare_scaled_coords(c, g, &sc_, s);
 }
 
@@ -317,6 +320,17 @@ int mgb_gauss_mixed_work(int n, int dim, const double* const* coords, long long*
   GaussSystem g;
   MGB_TRY(make_gauss_system(n, dim, coords, 0.0, MGB_NUGGET_DIAGONAL, &g));
   GaussMixedMatvec A;
+  MGB_TRY(A.init(c, g, c->stream));
+  *evaluated = A.evaluated();
+  return MGB_OK;
+}
+
+int mgb_gauss_fp64_work(int n, int dim, const double* const* coords, long long* evaluated) {
+  MGB_CTX(c);
+  if (!evaluated) return set_error(MGB_ERR_ARG, "mgb_gauss_fp64_work: null output");
+  GaussSystem g;
+  MGB_TRY(make_gauss_system(n, dim, coords, 0.0, MGB_NUGGET_DIAGONAL, &g));
+  GaussF64Matvec A;
   MGB_TRY(A.init(c, g, c->stream));
   *evaluated = A.evaluated();
   return MGB_OK;

@@ -274,11 +274,18 @@ __device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
 // the nugget.  The CTA map lists only groups with a near row tile, and a
 // 4-bit mask per CTA marks which of its row tiles are near; the slots of
 // far pairs are zeroed once and never written.
+//
+// The kernel is bound by its FMA pipe (3 packed instructions per entry, each
+// two pipe cycles), so occupancy is not what it lacks: with a minimum of one
+// CTA per SM in its launch bounds the compiler keeps more entries in flight
+// per warp (112 registers at d = 2, 4 CTAs per SM), 4 % faster on GB300 than
+// with registers capped for 6 or 7 CTAs per SM (0.207 against 0.215 ms for
+// the matvec at n = 65536, d = 2).
 constexpr int kGroup = 4;
 constexpr double kFarLog2 = 40.0;
 
 template <int DIM>
-__global__ void __launch_bounds__(kF32Threads) sym_f32_group_kernel(int n, int T, int GT,
+__global__ void __launch_bounds__(kF32Threads, 1) sym_f32_group_kernel(int n, int T, int GT,
                                                                     const int2* __restrict__ map,
                                                                     const float4* __restrict__ pts,
                                                                     const float* __restrict__ xf,

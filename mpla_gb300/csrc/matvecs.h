@@ -46,12 +46,15 @@ class GaussF64Matvec : public Matvec {
   int init(DeviceContext* c, const GaussSystem& g, cudaStream_t s);
   int apply(const double* x, double* y, cudaStream_t s, const int* skip) override;
   int n() const override { return g_.rows; }
+  // kernel entries one apply evaluates
+  long long evaluated() const { return evaluated_; }
 
  private:
   DeviceContext* c_ = nullptr;
   GaussSystem g_{};
   ScaledCoords sc_;
   Matvec* sym_ = nullptr;
+  long long evaluated_ = 0;
 };
 
 // Gaussian kernel matrix, FP32/SFU symmetric matvec (square systems).

@@ -90,6 +90,23 @@ def test_fp64_kernel_cu_rule_with_duplicate_points(gpu, orc):
     assert rel_err(dy.numpy(), op.matvec(x), abs_matvec(op, x)) <= 1e-13
 
 
+def test_fp64_matvec_far_pairs_left_out(gpu, orc):
+    # a short length scale: most tile pairs are farther apart than the FP64
+    # operator's 2^-80 cut and are not evaluated; the product must still meet
+    # the FP64 bar, and its work figure must show the cut
+    n, dim, ell = 8192, 2, 0.01
+    pts = scaled_points(n, dim, ell, seed=11)
+    x = np.random.default_rng(11).standard_normal(n)
+    dp = gpu.GaussPoints(pts)
+    dx, dy = gpu.DeviceArray.from_numpy(x), gpu.DeviceArray(n)
+    gpu.gauss_matvec_f64(dp, 1e-4, gpu.NUGGET_DIAGONAL, dx.ptr, dy.ptr)
+    gpu.synchronize()
+    op = orc.GaussOp(pts, 1e-4)
+    assert rel_err(dy.numpy(), op.matvec(x), abs_matvec(op, x)) <= 1e-13
+    half = (n // 128) * (n // 128 + 1) // 2 * 128 * 128
+    assert gpu.gauss_fp64_work(dp) < half // 2
+
+
 def test_fp64_far_points_underflow_to_zero(gpu):
     pts = np.array([[0.0, 40.0, 1e6], [0.0, 0.0, 0.0]])
     dp = gpu.GaussPoints(pts)
