@@ -38,8 +38,9 @@
 //   tile centres rounded once per pair, perturbs every tile pair
 //   differently; at n = 65536 that operator made the mixed solve stagnate at
 //   relres 1.4e-10, so coordinates are global.)  Exponentials on the SFU
-//   (ex2.approx, with coordinates pre-scaled by sqrt(log2 e)).  About 3.5
-//   issue slots of packed arithmetic and 1 MUFU per evaluated entry (d = 2).
+//   (ex2.approx, with coordinates pre-scaled by sqrt(log2 e)).  3 packed
+//   FMA-pipe instructions (6 FP32 lane operations) and 1 MUFU per evaluated
+//   entry (d = 2).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -499,11 +500,12 @@ std::vector<int> kd_tile_perm(const std::vector<double>& h, int n, int dim, int 
       }
     }
     const double* c = h.data() + (size_t)axis * n;
-    // a total order (coordinate, then index): the same split on every machine
-    std::sort(perm.begin() + r.lo, perm.begin() + r.hi,
-              [c](int a, int b) { return c[a] < c[b] || (c[a] == c[b] && a < b); });
     const int tiles = (cnt + leaf - 1) / leaf;
     const int mid = r.lo + (tiles / 2) * leaf;
+    // a total order (coordinate, then index): the left part is the same set
+    // of points on every machine, and each tile is sorted by index at the end
+    std::nth_element(perm.begin() + r.lo, perm.begin() + mid, perm.begin() + r.hi,
+                     [c](int a, int b) { return c[a] < c[b] || (c[a] == c[b] && a < b); });
     // the right half first on the stack, so the left half is laid out first
     stack.push_back({mid, r.hi});
     stack.push_back({r.lo, mid});
