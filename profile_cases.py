@@ -17,10 +17,13 @@ that ends by itself (a few hundred MB on the device at most):
   python profile_cases.py serving_sweep 0.2,0.4 32  # chosen rates and requests per rate
   python profile_cases.py all
 
-Prints the CUDA-event time per launch of each case.
+Prints the CUDA-event time per launch of each case.  The cases that write a
+record (batch_trace, serving_sweep) put it in the folder named by the
+environment variable PROFILE_OUT (default: profile_out).
 """
 from __future__ import annotations
 
+import os
 import sys
 from pathlib import Path
 
@@ -157,7 +160,10 @@ def case_batch128_solve():
     batch.close()
 
 
-def case_batch_trace(count=512, out="gpurun_out/batch_trace.csv"):
+OUT_DIR = Path(os.environ.get("PROFILE_OUT", "profile_out"))
+
+
+def case_batch_trace(count=512, out=None):
     """All `count` systems of the batch workload admitted together and run to
     relres 1e-10 one graph replay (8 steps) at a time: per replay the host
     wall time and the systems still running (a CSV), then the total, the
@@ -179,7 +185,8 @@ def case_batch_trace(count=512, out="gpurun_out/batch_trace.csv"):
         active = batch.run(max_steps=8)
         rows.append((len(rows), time.perf_counter() - t, active))
     sec = time.perf_counter() - t0
-    Path(out).parent.mkdir(parents=True, exist_ok=True)
+    out = Path(out) if out is not None else OUT_DIR / "batch_trace.csv"
+    out.parent.mkdir(parents=True, exist_ok=True)
     with open(out, "w") as f:
         f.write("replay,seconds,active\n")
         for r in rows:
@@ -200,7 +207,7 @@ def case_batch_trace(count=512, out="gpurun_out/batch_trace.csv"):
     batch.close()
 
 
-def case_serving_sweep(rates=(0.1, 0.2, 0.4), per_rate=32, out="gpurun_out/serving_sweep.json"):
+def case_serving_sweep(rates=(0.1, 0.2, 0.4), per_rate=32, out=None):
     """The serving configuration as specified: per arrival rate, Poisson
     arrivals of about `per_rate` requests, n log-uniform in [1024, 32768],
     d in {2,3}, l ~ U[0.03, 0.2], 1-4 N(0,1) right-hand sides, half FP64,
@@ -235,8 +242,9 @@ def case_serving_sweep(rates=(0.1, 0.2, 0.4), per_rate=32, out="gpurun_out/servi
             e.close()
         print(json.dumps(st), flush=True)
         res.append(st)
-    Path(out).parent.mkdir(parents=True, exist_ok=True)
-    Path(out).write_text(json.dumps(res, indent=1))
+    out = Path(out) if out is not None else OUT_DIR / "serving_sweep.json"
+    out.parent.mkdir(parents=True, exist_ok=True)
+    out.write_text(json.dumps(res, indent=1))
 
 
 def case_mixed_c3():
@@ -275,7 +283,7 @@ def main(argv):
         rates = tuple(float(r) for r in argv[1].split(","))
         per_rate = int(argv[2]) if len(argv) > 2 else 32
         case_serving_sweep(rates=rates, per_rate=per_rate,
-                           out=f"gpurun_out/serving_sweep_{argv[1].replace(',', '_')}.json")
+                           out=OUT_DIR / f"serving_sweep_{argv[1].replace(',', '_')}.json")
         mg.synchronize()
         return
     names = [k for k in CASES if k not in long_cases] if (not argv or argv[0] == "all") else argv
